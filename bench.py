@@ -1,0 +1,462 @@
+#!/usr/bin/env python
+"""Benchmark of the RBF-FD hot path on GB300.
+
+Workload (one GPU): N = 1024 x 1024 = 1,048,576 jittered nodes on [0,1]^2 (h = 2^-10,
+jitter +-0.3h, seed 1), PHS r^3, polynomial degree 3 (m = 10), k = 30 (s = 40); operators
+Dx, Dy and Lap = Dxx + Dyy.  One step = the hot path over that node set: grid build, kNN
+stencils, mixed-precision weight solves (FP32 LU, FP64 residual refinement, FP64 fallback)
+writing CSR, then one SpMV of each operator on a random N(0,1) field.  Inputs are resident
+in HBM when a step starts; L2 is flushed (256 MB write) before every step.
+
+value = weight solves per second (rows of all operators' local systems solved per second,
+whole job); the weights are verified against the FP64 GPU path over all rows and against
+the CPU oracle on a sample (<= 1e-9 max row-relative error).
+
+--impl reference: the reference algorithm's CPU path (the oracle port of the Julia code;
+Julia is not installed) timed on all host cores on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=1024, help="grid side per GPU (N = nx^2 rows per GPU)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+WORKLOAD = dict(p=3, n=30, deg=3, ops=("Dx", "Dy", "Lap"))
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def node_set(nx, ws):
+    """Global node set: nx columns x (nx * ws) rows; rank r owns rows [r*nx^2, (r+1)*nx^2)."""
+    import __graft_entry__
+
+    pkg = __graft_entry__.load_package()
+    X, h, _ = pkg.nodesets.jittered_grid(nx, nx * ws, 0.3, 1, box=((0.0, 1.0), (0.0, float(ws))))
+    return X, h
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "samples": len(sm),
+            "reasons": sorted(reasons),
+        }
+
+
+def cpu_sample_rate(X, target_s, nthreads=0, seed=0):
+    """Oracle (CPU restatement of the reference) weight solves per second on a random sample
+    of rows of the workload; the sample size is grown until it takes about target_s."""
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(seed)
+    p, n, deg, ops = WORKLOAD["p"], WORKLOAD["n"], WORKLOAD["deg"], WORKLOAD["ops"]
+    size = 2000
+    while True:
+        rows = np.sort(rng.choice(len(X), size, replace=False))
+        t0 = time.perf_counter()
+        orc.generate(X, X[rows], p, n, deg, ops, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s * 0.5 or size >= len(X):
+            return size / dt, size, dt
+        size = min(len(X), int(size * max(2.0, target_s / max(dt, 1e-3))))
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    from oracle import oracle as orc
+
+    X, _ = node_set(args.nx, 1)
+    cores = orc.max_threads()
+    rate0, size, dt = cpu_sample_rate(X, max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup)))
+    rng = np.random.default_rng(7)
+    p, n, deg, ops = WORKLOAD["p"], WORKLOAD["n"], WORKLOAD["deg"], WORKLOAD["ops"]
+    times = []
+    for it in range(args.warmup + args.steps):
+        rows = np.sort(rng.choice(len(X), size, replace=False))
+        t0 = time.perf_counter()
+        orc.generate(X, X[rows], p, n, deg, ops)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.mean(times))
+    value = size / (ms * 1e-3)
+    sample = (f"{size} random rows of the {len(X)}-node workload per step (stencils, explicit "
+              f"inverse of the 40x40 system, weights of Dx/Dy/Lap), C oracle port, {cores} threads")
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "weight solves/s (N=1,048,576, k=30, deg 3, PHS r^3; Dx, Dy, Lap)",
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded jittered grid)",
+        "config": {"workload": "1024x1024 jittered nodes, p=3, deg=3, k=30, ops Dx,Dy,Lap", "rows_per_step": size},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def row_rel_err(a, b, n):
+    """max over rows of ||a_i - b_i||_inf / ||b_i||_inf for row-major (rows, n) torch tensors."""
+    import torch
+
+    a = a.view(-1, n)
+    b = b.view(-1, n)
+    num = (a - b).abs().amax(1)
+    den = b.abs().amax(1)
+    return float((num / den).max().item()), float((num / den).median().item())
+
+
+def run_ours(args):
+    import torch
+
+    import __graft_entry__
+
+    pkg = __graft_entry__.load_package()
+    nat = pkg._native
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    L = nat.load()
+    h = pkg.Handle(device=local)
+    st_ptr = h.stream
+    stream = torch.cuda.ExternalStream(st_ptr)
+    p, n, deg, ops = WORKLOAD["p"], WORKLOAD["n"], WORKLOAD["deg"], WORKLOAD["ops"]
+    X_host, hgrid = node_set(args.nx, ws)
+    N = len(X_host)
+    rows_per = args.nx * args.nx
+    rb, re = rank * rows_per, (rank + 1) * rows_per
+    fp64_peak, fp32_peak = ctypes.c_double(), ctypes.c_double()
+    L.rbffd_measure_fma_peaks(local, ctypes.byref(fp64_peak), ctypes.byref(fp32_peak))
+
+    with torch.cuda.stream(stream):
+        Xd = torch.tensor(X_host, device="cuda")
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(1234)
+        xfield = torch.randn(N, dtype=torch.float64, device="cuda", generator=gen)
+        ys = [torch.empty(rows_per, dtype=torch.float64, device="cuda") for _ in ops]
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream.synchronize()
+
+    def opset(precision):
+        return pkg.OperatorSet(Xd, None, p, n, deg, ops=ops, precision=precision, row_range=(rb, re), handle=h,
+                               device=True)
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def step(precision, collect):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        s = opset(precision)
+        for q, o in enumerate(ops):
+            s.spmv_ptr(o, xfield.data_ptr(), ys[q].data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        collect.append((e0.elapsed_time(e1), s.stats.as_dict()))
+        s.close()
+
+    # ---- verification (untimed): mixed vs FP64 GPU over all rows, both vs the oracle on a sample
+    s64 = opset("fp64")
+    smx = opset("mixed")
+    err_all = {}
+    for q, o in enumerate(ops):
+        with torch.cuda.stream(stream):
+            err_all[o] = row_rel_err(smx.device_values(o), s64.device_values(o), n)
+    mixed_stats = smx.stats.as_dict()
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(3)
+    sample = np.sort(rng.choice(np.arange(rb, re), 2000, replace=False))
+    ref = orc.generate(X_host, X_host[sample], p, n, deg, ops)
+    err_oracle = {}
+    for q, o in enumerate(ops):
+        for name, s in (("fp64", s64), ("mixed", smx)):
+            _, _, val = s.csr_arrays(o)
+            W = val.reshape(-1, n)[sample - rb]
+            e = np.abs(W - ref["W"][q]).max(1) / np.abs(ref["W"][q]).max(1)
+            err_oracle[f"{name}_{o}"] = float(e.max())
+    s64.close()
+    smx.close()
+
+    # ---- timed steps (mixed = the metric), then the FP64 form for the ratio
+    for _ in range(args.warmup):
+        step("mixed", [])
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    t_wall = time.perf_counter()
+    timed = []
+    for _ in range(args.steps):
+        step("mixed", timed)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = clk.stop()
+    ms_step = float(np.mean([t for t, _ in timed]))
+    if dist:
+        tt = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    total_rows = rows_per * ws
+    value = total_rows / (ms_step * 1e-3)
+
+    fp64_steps = []
+    for _ in range(1):
+        step("fp64", [])
+    for _ in range(max(2, args.steps // 2)):
+        step("fp64", fp64_steps)
+    ms_fp64 = float(np.mean([t for t, _ in fp64_steps]))
+
+    # ---- kernel-level numbers: solve kernel (from the library's events) and SpMV
+    st_mixed = [s for _, s in timed]
+    solve_ms = float(np.mean([s["ms_solve"] for s in st_mixed]))
+    knn_ms = float(np.mean([s["ms_knn"] for s in st_mixed]))
+    solve_ms_fp64 = float(np.mean([s["ms_solve"] for _, s in fp64_steps]))
+    s = opset("mixed")
+    spmv_times = []
+    for it in range(12):
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        s.spmv_ptr("Lap", xfield.data_ptr(), ys[2].data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        if it >= 2:
+            spmv_times.append(e0.elapsed_time(e1))
+    spmv_ms = float(np.mean(spmv_times))
+    nnz = s.nnz
+    spmv_bytes = nnz * (8 + 4) + (rows_per + 1) * 8 + N * 8 + rows_per * 8
+    spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    s.close()
+
+    # ---- e2e: the drop-in C-ABI call with host buffers (H2D of X, D2H of the CSC operators)
+    e2e = None
+    if not args.no_e2e and ws == 1:
+        mask = sum(1 << nat.OP_CODES[o] for o in ops)
+        pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True)  # noqa: E731
+        Xp = pin((N, 2), torch.float64)
+        Xp.copy_(torch.from_numpy(X_host))
+        outs = (nat.CSC * len(ops))()
+        keep = []
+        for q in range(len(ops)):
+            cp, rv, nz = pin(N + 1, torch.int64), pin(N * n, torch.int64), pin(N * n, torch.float64)
+            keep += [cp, rv, nz]
+            outs[q].colptr, outs[q].rowval, outs[q].nzval = cp.data_ptr(), rv.data_ptr(), nz.data_ptr()
+        est = nat.Stats()
+        e2e_t = []
+        for it in range(1 + max(2, args.steps // 2)):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            stream.synchronize()
+            t0 = time.perf_counter()
+            rc = L.rbffd_generate_operator(h.ptr, ctypes.c_void_p(Xp.data_ptr()), N, ctypes.c_void_p(Xp.data_ptr()),
+                                           N, p, n, deg, None, mask, nat.PREC["mixed"], outs, ctypes.byref(est))
+            dt = time.perf_counter() - t0
+            nat.check(h.ptr, rc)
+            if it >= 1:
+                e2e_t.append(dt)
+        ms_e2e = 1e3 * float(np.mean(e2e_t))
+        e2e = {
+            "value": N / (ms_e2e * 1e-3),
+            "unit": "solves/s",
+            "ms_per_call": ms_e2e,
+            "h2d_bytes_per_step": N * 16,
+            "d2h_bytes_per_step": len(ops) * (N * n * 16 + (N + 1) * 8),
+            "call": "rbffd_generate_operator (host X in, caller-allocated pinned CSC out, Dx/Dy/Lap, mixed)",
+        }
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---- CPU baseline (oracle port, host cores, bounded sample)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as orc
+
+        rate, size, dt = cpu_sample_rate(X_host[: rows_per] if ws == 1 else X_host, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "solves/s", "cores": orc.max_threads(), "kind": "port",
+               "sample": f"{size} random rows of the {rows_per}-node workload (kNN, explicit inverse, Dx/Dy/Lap "
+                         f"weights), C oracle port, {dt:.1f} s"}
+
+    m = 10
+    s_ = n + m
+    # FP64 work of the mixed solve per system: FP64 assembly of A (pairs: 2 sub, mul, fma,
+    # sqrt ~ counted as 1, r^2*r mul), RHS, and each refinement residual 2*(s^2 - m^2)*r.
+    hist = mixed_stats["refine_hist"]
+    nres = sum(i * c for i, c in enumerate(hist)) / max(1, sum(hist))
+    fp64_flops_sys = (n * (n - 1) / 2) * 6 + n * m * 2 + n * 3 * 12 + nres * 2 * (s_ * s_ - m * m) * 3
+    solve_ach = rows_per * fp64_flops_sys / (solve_ms * 1e-3) / 1e12
+    hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs") if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800 GB/s"
+    hbm = hbm or 6800.0
+    out = {
+        "metric": "weight solves/s at <=1e-9 rel err (FP32+refine vs FP64); stencil-apply HBM GB/s",
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded jittered grid, splitmix64)",
+        "config": {
+            "workload": f"{args.nx}x{args.nx} jittered nodes per GPU (h=1/{args.nx}, +-0.3h), PHS r^3, deg 3 (m=10), "
+                        f"k=30 (s=40), ops Dx,Dy,Lap; step = grid+kNN+mixed solves+CSR + 1 SpMV per op",
+            "rows_per_gpu": rows_per,
+            "l2": "flushed (256 MB write) before every step",
+            "parallelism": f"row shards x{ws}" if ws > 1 else "single GPU",
+        },
+        "e2e": e2e,
+        "gpu_launches": int(np.mean([s["kernel_launches"] for s in st_mixed])) + len(ops),
+        "clocks": clocks,
+        "wall_s_timed_region": wall,
+        "accuracy": {
+            "max_row_rel_err_mixed_vs_fp64_gpu_all_rows": {o: v[0] for o, v in err_all.items()},
+            "median_row_rel_err_mixed_vs_fp64_gpu": {o: v[1] for o, v in err_all.items()},
+            "max_row_rel_err_vs_oracle_2000_rows": err_oracle,
+            "fallback_fraction": mixed_stats["n_fallback"] / max(1, mixed_stats["n_systems"]),
+            "refine_hist": hist,
+        },
+        "fp64_form": {"value": rows_per * ws / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64,
+                      "solve_kernel_ms": solve_ms_fp64},
+        "mixed_over_fp64": ms_fp64 / ms_step,
+        "phases_ms": {"knn": knn_ms, "solve_mixed": solve_ms, "spmv_per_op": spmv_ms,
+                      "grid": float(np.mean([s["ms_grid"] for s in st_mixed]))},
+        "measured_fma_peaks_tflops": {"fp64": fp64_peak.value, "fp32": fp32_peak.value},
+        "roofline": {
+            "kernel": "solve_mixed_kernel",
+            "bound": "fp64",
+            "achieved": solve_ach,
+            "peak": fp64_peak.value,
+            "unit": "TFLOP/s",
+            "frac": solve_ach / fp64_peak.value if fp64_peak.value else None,
+            "traffic": None,
+            "note": "FP64 work of the mixed solve (A assembly, RHS, refinement residuals) over the kernel's "
+                    "event-timed duration, against the measured FP64 FMA peak (rbffd_measure_fma_peaks)",
+        },
+        "roofline_apply": {
+            "kernel": "spmv_f64_kernel",
+            "bound": "hbm",
+            "achieved": spmv_gbs,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": spmv_gbs / hbm,
+            "traffic": None,
+            "algorithmic_bytes": spmv_bytes,
+            "peak_source": hbm_src,
+        },
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

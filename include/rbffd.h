@@ -1,0 +1,219 @@
+/*
+ * rbffd.h -- C ABI of the GB300-native RBF-FD hot path.
+ *
+ * Drop-in boundary for RadialBasisFiniteDifferences.jl (v0.1.0).  The Julia host keeps
+ * its public API (generate_operator, hyperviscosity_operator, calculateneighbors) and
+ * ccalls the entry points below, which run kNN stencil selection, the per-node local
+ * RBF-FD weight solves and the sparse operator build on one sm_103a GPU and hand back
+ * the same SparseMatrixCSC{Float64,Int64} data (1-based colptr/rowval, nzval, explicit
+ * zeros kept).  Device-resident operator sets (rbffd_opset_*) serve time stepping:
+ * SpMV / multi-field SpMM and RK4 stages captured in a CUDA graph.
+ *
+ * Conventions
+ *   - Points are AoS doubles (x0,y0,x1,y1,...): the memory layout of Julia's
+ *     Vector{SVector{2,Float64}}.
+ *   - node_class (nullable, N entries) encodes the index ranges of the boundary-aware
+ *     overloads: 0 interior (X_idx_in), +b boundary b (X_idx_bc[b]), -b ghost of
+ *     boundary b (X_idx_bc_g[b]), b = 1, 2, ...
+ *   - Output buffers are caller-allocated; every call returns an rbffd_status.
+ *   - One handle per host thread.  Calls on one handle are serialised on the handle's
+ *     CUDA stream; a handle is not re-entrant.
+ *   - No entry point falls back to the CPU.  Without a usable sm_103a GPU every call
+ *     returns RBFFD_ECUDA.
+ */
+#ifndef RBFFD_H
+#define RBFFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RBFFD_VERSION_MAJOR 0
+#define RBFFD_VERSION_MINOR 1
+
+typedef enum {
+    RBFFD_OK = 0,
+    RBFFD_EINVAL = 1,    /* bad argument: sizes, k > #candidates, NaN coordinates, ... */
+    RBFFD_ECUDA = 2,     /* CUDA runtime failure or no usable GPU */
+    RBFFD_ESINGULAR = 3, /* a local system is singular (stats.first_bad_node) */
+    RBFFD_ETIMEOUT = 4,  /* a bounded device wait gave up */
+    RBFFD_ENOMEM = 5     /* device or host allocation failed */
+} rbffd_status;
+
+/* Operators (bit i of an op mask <-> operator code i).  The reference's generate_operator
+   returns (E, Dx, Dy, Dxx, Dyy, Dxy) (src/generate_operator.jl:189); hyperviscosity_operator
+   returns (Dxk, Dyk) (src/hyperviscosity_operator.jl:174).  LAP = Dxx + Dyy and
+   HV = Dxk + Dyk are solved from one combined right-hand side. */
+enum {
+    RBFFD_OP_E = 0,
+    RBFFD_OP_DX = 1,
+    RBFFD_OP_DY = 2,
+    RBFFD_OP_DXX = 3,
+    RBFFD_OP_DYY = 4,
+    RBFFD_OP_DXY = 5,
+    RBFFD_OP_LAP = 6,
+    RBFFD_OP_DXK = 7,
+    RBFFD_OP_DYK = 8,
+    RBFFD_OP_HV = 9,
+    RBFFD_OP_COUNT = 10
+};
+#define RBFFD_MASK(op) (1u << (op))
+#define RBFFD_MASK_GENERATE                                                                   \
+    (RBFFD_MASK(RBFFD_OP_E) | RBFFD_MASK(RBFFD_OP_DX) | RBFFD_MASK(RBFFD_OP_DY) |             \
+     RBFFD_MASK(RBFFD_OP_DXX) | RBFFD_MASK(RBFFD_OP_DYY) | RBFFD_MASK(RBFFD_OP_DXY))
+#define RBFFD_MASK_HYPERVISCOSITY (RBFFD_MASK(RBFFD_OP_DXK) | RBFFD_MASK(RBFFD_OP_DYK))
+
+/* Precision of the local solves. */
+enum {
+    RBFFD_PREC_FP64 = 0,  /* assemble, LU-factor and solve in FP64 */
+    RBFFD_PREC_MIXED = 1  /* FP32 assembly + LU on the scaled stencil, FP64 residuals and
+                             iterative refinement, per-stencil FP64 fallback when it stalls */
+};
+
+/* Where pointers passed to rbffd_opset_create live. */
+enum { RBFFD_MEM_HOST = 0, RBFFD_MEM_DEVICE = 1 };
+
+typedef struct rbffd_handle rbffd_handle;
+typedef struct rbffd_opset rbffd_opset;
+typedef struct rbffd_rk4 rbffd_rk4;
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    int warps_per_block; /* weight-solve CTA size in warps; 0 = autotune */
+    int max_refine;      /* mixed precision: refinement iterations before fallback (0 = 6) */
+    double refine_tol;   /* mixed precision: stop when the predicted relative weight error
+                            is below this (0 = 1e-12) */
+} rbffd_options;
+
+typedef struct {
+    double ms_upload, ms_grid, ms_knn, ms_solve, ms_fallback, ms_csr, ms_total;
+    int64_t n_systems;      /* local systems factored */
+    int64_t n_rows;         /* operator rows (evaluation points) */
+    int64_t n_fallback;     /* mixed: systems re-solved in FP64 */
+    int64_t first_bad_node; /* 0-based X node of the first singular system, -1 if none */
+    int64_t refine_hist[8]; /* mixed: systems that converged after i refinement steps */
+    int64_t nnz;            /* nonzeros per operator */
+    int64_t kernel_launches;/* CUDA kernels this call launched */
+} rbffd_stats;
+
+/* Caller-owned CSC arrays of one operator (Julia SparseMatrixCSC{Float64,Int64}). */
+typedef struct {
+    int64_t *colptr; /* ncols + 1, 1-based */
+    int64_t *rowval; /* nnz, 1-based, ascending within each column */
+    double *nzval;   /* nnz */
+} rbffd_csc;
+
+/* Problem description of rbffd_opset_create. */
+typedef struct {
+    const double *X; /* N interpolation nodes (AoS) */
+    int64_t N;
+    const double *Y; /* M evaluation points (AoS); NULL = collocated (Y = X) */
+    int64_t M;
+    int p;                      /* PHS exponent (odd, r^p) */
+    int n;                      /* stencil size (uniform; ignored if n_per_node) */
+    int polydeg;                /* polynomial degree (uniform; ignored if deg_per_node) */
+    const int32_t *node_class;  /* nullable, see Conventions */
+    const int32_t *n_per_node;  /* nullable: per-node stencil size */
+    const int32_t *deg_per_node;/* nullable: per-node polynomial degree */
+    uint32_t op_mask;           /* operators to build */
+    int k_deriv;                /* derivative order of DXK/DYK/HV */
+    int precision;              /* RBFFD_PREC_* */
+    int memspace;               /* RBFFD_MEM_* of X, Y, node_class, n/deg arrays */
+    int64_t row_begin, row_end; /* evaluation rows [row_begin,row_end) to build (sharding);
+                                   row_end <= 0 means all rows */
+} rbffd_problem;
+
+int rbffd_version(void);
+const char *rbffd_status_string(int status);
+
+int rbffd_create(const rbffd_options *opt, rbffd_handle **out);
+void rbffd_destroy(rbffd_handle *h);
+/* Text of the last error on this handle (never NULL). */
+const char *rbffd_last_error(const rbffd_handle *h);
+/* The handle's cudaStream_t, as void*. */
+void *rbffd_stream(rbffd_handle *h);
+int rbffd_synchronize(rbffd_handle *h);
+
+/* ---------------------------------------------------------------------------------
+ * Drop-in entry points (host buffers in, caller-allocated host CSC out).
+ * ------------------------------------------------------------------------------ */
+
+/* generate_operator(X, Y, p, n, polydeg) -- src/generate_operator.jl:29-190 -- and, with
+   node_class != NULL, the boundary-aware overload generate_operator(X, Y, p, n, polydeg,
+   X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc, Y_idx_bc_g) -- :192-352.
+   out[] has one rbffd_csc per set bit of op_mask, in increasing bit order; each is an
+   M x N matrix with nnz = M * n.  Y == X (same pointer, M == N) is the collocated case. */
+int rbffd_generate_operator(rbffd_handle *h, const double *X, int64_t N, const double *Y,
+                            int64_t M, int p, int n, int polydeg, const int32_t *node_class,
+                            uint32_t op_mask, int precision, rbffd_csc *out,
+                            rbffd_stats *stats);
+
+/* hyperviscosity_operator(k_deriv, X, Y, p, n, polydeg[, index ranges]) --
+   src/hyperviscosity_operator.jl:26-175 and :177-312.  out[0] = Dxk, out[1] = Dyk. */
+int rbffd_hyperviscosity_operator(rbffd_handle *h, int k_deriv, const double *X, int64_t N,
+                                  const double *Y, int64_t M, int p, int n, int polydeg,
+                                  const int32_t *node_class, int precision, rbffd_csc *out,
+                                  rbffd_stats *stats);
+
+/* The collocated, unscaled overloads generate_operator(X, p, n, polydeg)
+   (src/generate_operator.jl:354-491) and hyperviscosity_operator(k, X, p, n, polydeg)
+   (src/hyperviscosity_operator.jl:314-440), reproduced as the reference computes them:
+   no stencil scaling, centre shifted to (eps, eps), RBF right-hand side evaluated at
+   x_j - x_c.  k_deriv is used when op_mask holds DXK/DYK/HV. */
+int rbffd_generate_operator_unscaled(rbffd_handle *h, const double *X, int64_t N, int p, int n,
+                                     int polydeg, uint32_t op_mask, int k_deriv,
+                                     rbffd_csc *out, rbffd_stats *stats);
+
+/* calculateneighbors(X, Y, n, X_idx_in, X_idx_bc, X_idx_bc_g, ...) --
+   src/calculateneighbors.jl:1-97 (node_class == NULL: the plain knn of
+   src/generate_operator.jl:43-47).  idxs_x: N x n 1-based ids sorted by distance (self
+   first); dists_x: N x n Euclidean distances (nullable); idxs_y_x / dists_y_x: nearest
+   node of each Y point (nullable when M == 0). */
+int rbffd_calculateneighbors(rbffd_handle *h, const double *X, int64_t N, const double *Y,
+                             int64_t M, int n, const int32_t *node_class, int64_t *idxs_x,
+                             double *dists_x, int64_t *idxs_y_x, double *dists_y_x);
+
+/* ---------------------------------------------------------------------------------
+ * Device-resident operator sets (time stepping, benchmarks).
+ * ------------------------------------------------------------------------------ */
+
+int rbffd_opset_create(rbffd_handle *h, const rbffd_problem *prob, rbffd_opset **out,
+                       rbffd_stats *stats);
+void rbffd_opset_destroy(rbffd_handle *h, rbffd_opset *s);
+/* Shape: rows (evaluation points built), cols (N), nnz per operator, op count. */
+int rbffd_opset_shape(const rbffd_opset *s, int64_t *rows, int64_t *cols, int64_t *nnz,
+                      int *nops);
+/* Device CSR of operator `op` (its index among the set's ops): row_ptr (rows+1, int64),
+   col (nnz, int32 0-based), val (nnz, double).  Pointers stay owned by the set. */
+int rbffd_opset_device_csr(const rbffd_opset *s, int op, const int64_t **row_ptr,
+                           const int32_t **col, const double **val);
+/* Copy one operator to caller-allocated host CSC (1-based, Julia layout). */
+int rbffd_opset_export_csc(rbffd_handle *h, rbffd_opset *s, int op, rbffd_csc *out);
+/* Copy one operator to caller-allocated host CSR (0-based int64 row_ptr / int32 col). */
+int rbffd_opset_export_csr(rbffd_handle *h, rbffd_opset *s, int op, int64_t *row_ptr,
+                           int32_t *col, double *val);
+/* Copy the stencils (N x n 0-based, uniform n only) and nearest-node ids of the rows. */
+int rbffd_opset_export_stencils(rbffd_handle *h, rbffd_opset *s, int32_t *nbr, int32_t *nn);
+
+/* y = A_op x on the handle's stream; x, y device pointers (FP64, cols / rows long). */
+int rbffd_spmv(rbffd_handle *h, rbffd_opset *s, int op, const double *x, double *y);
+/* Y = A_op X for nfields fields, X row-major [cols][nfields], Y [rows][nfields];
+   dtype 0 = FP64 weights and fields, 1 = FP32 weights and fields. */
+int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, int nfields,
+               int dtype);
+
+/* ---------------------------------------------------------------------------------
+ * Diagnostics.
+ * ------------------------------------------------------------------------------ */
+
+/* Measured FP64 and FP32 CUDA-core FMA throughput of `device` in TFLOP/s (the peaks that
+   bound the weight solves; no reference counterpart). */
+int rbffd_measure_fma_peaks(int device, double *fp64_tflops, double *fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RBFFD_H */

@@ -1,0 +1,1033 @@
+// C ABI of librbffd (include/rbffd.h): handles, device-resident operator sets and the
+// drop-in entry points that mirror RadialBasisFiniteDifferences.jl's public functions.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "rbffd_internal.cuh"
+
+#define RBFFD_EXPORT extern "C" __attribute__((visibility("default")))
+
+struct rbffd_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    rbffd_options opt{};
+    std::string err;
+    int num_sms = 0;
+    cudaEvent_t ev[8] = {};
+};
+
+struct rbffd_opset {
+    int64_t N = 0, M = 0, rows = 0, row_begin = 0, nnz = 0;
+    int nops = 0;
+    int ops[RBFFD_OP_COUNT] = {};
+    bool collocated = true, uniform = true;
+    int n = 0;
+    double2 *X = nullptr;
+    int32_t *nbr = nullptr;
+    int64_t *nbr_ptr = nullptr;
+    int32_t *nn = nullptr;  // X node of each row
+    int64_t *row_ptr = nullptr;
+    int32_t *col = nullptr;
+    double *val = nullptr;
+    float *val32 = nullptr;
+    int64_t *csc_colptr = nullptr, *csc_rowval = nullptr, *csc_perm = nullptr;
+    double *csc_tmp = nullptr;
+    std::vector<void *> owned;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(rbffd_handle *h, int code, const std::string &msg)
+{
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CK(expr)                                                                               \
+    do {                                                                                       \
+        cudaError_t _e = (expr);                                                               \
+        if (_e != cudaSuccess)                                                                 \
+            return fail(h, _e == cudaErrorMemoryAllocation ? RBFFD_ENOMEM : RBFFD_ECUDA,       \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));                   \
+    } while (0)
+
+// Stream-ordered device allocations that are released together.
+struct Arena {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit Arena(cudaStream_t s) : st(s) {}
+    template <typename T>
+    cudaError_t get(T **p, size_t count)
+    {
+        void *q = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&q, bytes, st);
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(q);
+        *p = (T *)q;
+        return cudaSuccess;
+    }
+    template <typename T>
+    cudaError_t zeros(T **p, size_t count)
+    {
+        cudaError_t e = get(p, count);
+        if (e != cudaSuccess) return e;
+        return cudaMemsetAsync(*p, 0, std::max<size_t>(count * sizeof(T), 16), st);
+    }
+    void release_to(std::vector<void *> &dst)
+    {
+        dst.insert(dst.end(), ptrs.begin(), ptrs.end());
+        ptrs.clear();
+    }
+    ~Arena()
+    {
+        for (void *p : ptrs) cudaFreeAsync(p, st);
+    }
+};
+
+__global__ void iota_i32(int32_t *a, int64_t n, int64_t base)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = (int32_t)(base + i);
+}
+
+__global__ void uniform_ptr(int64_t *a, int64_t n, int64_t step)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = i * step;
+}
+
+__global__ void mark_nodes(const int32_t *nn, int64_t rows, int64_t *flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+        flag[nn[i]] = 1;
+}
+
+__global__ void compact_nodes(const int64_t *flag, const int64_t *pos, int64_t N, int32_t *sys_node)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) sys_node[pos[i]] = (int32_t)i;
+}
+
+__global__ void count_rows(const int32_t *nn, int64_t rows, const int64_t *pos, unsigned long long *cnt)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[pos[nn[i]]], 1ull);
+}
+
+__global__ void scatter_rows(const int32_t *nn, int64_t rows, int64_t row_begin, const int64_t *pos,
+                             const int64_t *start, unsigned long long *fill, int32_t *rows_list)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = pos[nn[i]];
+        int64_t at = start[s] + (int64_t)atomicAdd(&fill[s], 1ull);
+        rows_list[at] = (int32_t)(row_begin + i);
+    }
+}
+
+// Rows of one system are written in any order; make the order deterministic (ascending).
+__global__ void sort_row_lists(const int64_t *start, int64_t nsys, int32_t *rows_list)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nsys; s += (int64_t)gridDim.x * blockDim.x) {
+        int64_t a = start[s], b = start[s + 1];
+        for (int64_t i = a + 1; i < b; i++) {
+            int32_t v = rows_list[i];
+            int64_t j = i - 1;
+            while (j >= a && rows_list[j] > v) {
+                rows_list[j + 1] = rows_list[j];
+                j--;
+            }
+            rows_list[j + 1] = v;
+        }
+    }
+}
+
+__global__ void row_len_kernel(const int32_t *nn, int64_t rows, const int32_t *n_node, int n_uni,
+                               int64_t *len)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+        len[i] = n_node ? n_node[nn[i]] : n_uni;
+}
+
+__global__ void i32_to_i64(const int32_t *a, int64_t *b, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+
+__global__ void knn_export(const int32_t *idx, const double *d2, int64_t n, int64_t *oidx, double *odist)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        oidx[i] = (int64_t)idx[i] + 1;
+        if (odist) odist[i] = sqrt(d2[i]);
+    }
+}
+
+int nblk(int64_t n, int t = 256)
+{
+    int64_t b = (n + t - 1) / t;
+    if (b < 1) b = 1;
+    if (b > 65535 * 8) b = 65535 * 8;
+    return (int)b;
+}
+
+int npoly_h(int d) { return (d + 1) * (d + 2) / 2; }
+
+double ff_h(double x, int q)
+{
+    double c = 1.0;
+    for (int t = 0; t < q; t++) c *= (x - t);
+    return c;
+}
+
+double fact_h(int n)
+{
+    double f = 1;
+    for (int i = 2; i <= n; i++) f *= i;
+    return f;
+}
+
+bool comp_terms(int p, int a, int b, OpComp *c)
+{
+    c->a = a;
+    c->b = b;
+    c->nterm = 0;
+    for (int i = 0; 2 * i <= a; i++)
+        for (int j = 0; 2 * j <= b; j++) {
+            int q = a + b - i - j;
+            double coef = fact_h(a) / (fact_h(i) * fact_h(a - 2 * i)) * fact_h(b) /
+                          (fact_h(j) * fact_h(b - 2 * j)) * ldexp(1.0, a - 2 * i + b - 2 * j) *
+                          ff_h(0.5 * p, q);
+            if (coef == 0.0) continue;
+            if (c->nterm >= RBFFD_MAX_TERMS) return false;
+            c->t[c->nterm++] = RbfTerm{coef, a - 2 * i, b - 2 * j, p - 2 * q};
+        }
+    return true;
+}
+
+// Host copies of small per-node arrays (for sizing / validation).
+bool fetch_i32(rbffd_handle *h, const int32_t *src, int64_t n, int memspace, std::vector<int32_t> &dst)
+{
+    dst.resize(n);
+    if (memspace == RBFFD_MEM_DEVICE) {
+        if (cudaMemcpyAsync(dst.data(), src, n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+            return false;
+        return cudaStreamSynchronize(h->stream) == cudaSuccess;
+    }
+    memcpy(dst.data(), src, n * sizeof(int32_t));
+    return true;
+}
+
+// Upload (or borrow) an array of `bytes`; device pointers are used in place when aligned.
+template <typename T>
+cudaError_t stage(rbffd_handle *h, Arena &ar, const void *src, size_t count, int memspace, T **dst)
+{
+    if (memspace == RBFFD_MEM_DEVICE && ((uintptr_t)src % alignof(T)) == 0) {
+        *dst = (T *)src;
+        return cudaSuccess;
+    }
+    cudaError_t e = ar.get(dst, count);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(*dst, src, count * sizeof(T),
+                           memspace == RBFFD_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           h->stream);
+}
+
+struct GridBuild {
+    GridDev g{};
+    int64_t ncell = 0;
+    double rho = 1;
+};
+
+int build_grid(rbffd_handle *h, Arena &ar, const double2 *dX, const int32_t *dcls, int64_t N, GridBuild &gb)
+{
+    const int nb = 256;
+    double *partial, *box;
+    int *bad;
+    CK(ar.get(&partial, 4 * nb));
+    CK(ar.get(&box, 4));
+    CK(ar.get(&bad, 1));
+    CK(launch_bbox(dX, N, partial, nb, box, bad, h->stream));
+    double hb[4];
+    int hbad = 0;
+    CK(cudaMemcpyAsync(hb, box, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (hbad) return fail(h, RBFFD_EINVAL, "non-finite node coordinates");
+    double w = hb[1] - hb[0], hh = hb[3] - hb[2];
+    double area = (w > 0 ? w : 1.0) * (hh > 0 ? hh : 1.0);
+    double cs = sqrt(2.0 * area / (double)N);
+    if (!(cs > 0)) cs = 1.0;
+    int64_t nx = (int64_t)(w / cs) + 1, ny = (int64_t)(hh / cs) + 1;
+    while (nx * ny > 4 * N + 16) {
+        cs *= 1.5;
+        nx = (int64_t)(w / cs) + 1;
+        ny = (int64_t)(hh / cs) + 1;
+    }
+    int64_t ncell = nx * ny;
+    int64_t *count, *start64;
+    int32_t *cell_of, *start32, *fill, *ids, *gcls = nullptr;
+    double2 *pts;
+    void *tmp;
+    size_t tb = scan_tmp_bytes(ncell);
+    CK(ar.zeros(&count, ncell + 1));
+    CK(ar.get(&start64, ncell + 1));
+    CK(ar.get(&cell_of, N));
+    CK(ar.get(&start32, ncell + 1));
+    CK(ar.get(&fill, ncell));
+    CK(ar.get(&ids, N));
+    CK(ar.get(&pts, N));
+    if (dcls) CK(ar.get(&gcls, N));
+    CK(ar.get((char **)&tmp, tb));
+    CK(launch_grid_fill(dX, dcls, N, hb[0], hb[2], cs, (int)nx, (int)ny, count, cell_of, h->stream));
+    CK(scan_exclusive_i64(count, start64, ncell, tmp, tb, h->stream));
+    CK(launch_grid_scatter(dX, dcls, N, cell_of, start64, start32, ncell, fill, pts, ids, gcls, h->stream));
+    gb.g = GridDev{hb[0], hb[2], cs, (int)nx, (int)ny, start32, pts, ids, gcls};
+    gb.ncell = ncell;
+    gb.rho = (double)N / (double)ncell;
+    return RBFFD_OK;
+}
+
+int knn_r0(double rho, int k)
+{
+    double r = (sqrt((double)k / (rho > 0 ? rho : 1.0)) - 1.0) * 0.5;
+    int r0 = (int)ceil(r);
+    return r0 < 0 ? 0 : r0;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+struct Flags {
+    int knn_err;
+    int fallback_count;
+    int64_t first_bad;
+    unsigned long long hist[8];
+};
+
+int ops_from_mask(uint32_t mask, int *ops)
+{
+    int n = 0;
+    for (int b = 0; b < RBFFD_OP_COUNT; b++)
+        if (mask & (1u << b)) ops[n++] = b;
+    return n;
+}
+
+int autotune_wpb(rbffd_handle *h, size_t per_warp)
+{
+    if (h->opt.warps_per_block > 0) return h->opt.warps_per_block;
+    // Largest CTA (<= 8 warps) whose shared memory still lets >= 2 CTAs share an SM.
+    const size_t budget = 110 * 1024;
+    int w = 8;
+    while (w > 1 && per_warp * w > budget) w >>= 1;
+    return w;
+}
+
+}  // namespace
+
+bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, std::string *err)
+{
+    memset(t, 0, sizeof(*t));
+    t->nops = nops;
+    t->p = p;
+    for (int q = 0; q < nops; q++) {
+        OpDesc &d = t->op[q];
+        int code = ops[q];
+        int comps[2][2] = {{0, 0}, {0, 0}};
+        d.ncomp = 1;
+        switch (code) {
+        case RBFFD_OP_E: break;
+        case RBFFD_OP_DX: comps[0][0] = 1; break;
+        case RBFFD_OP_DY: comps[0][1] = 1; break;
+        case RBFFD_OP_DXX: comps[0][0] = 2; break;
+        case RBFFD_OP_DYY: comps[0][1] = 2; break;
+        case RBFFD_OP_DXY: comps[0][0] = 1; comps[0][1] = 1; break;
+        case RBFFD_OP_LAP: comps[0][0] = 2; comps[1][1] = 2; d.ncomp = 2; break;
+        case RBFFD_OP_DXK: comps[0][0] = k_deriv; break;
+        case RBFFD_OP_DYK: comps[0][1] = k_deriv; break;
+        case RBFFD_OP_HV: comps[0][0] = k_deriv; comps[1][1] = k_deriv; d.ncomp = 2; break;
+        default: *err = "unknown operator code"; return false;
+        }
+        d.post_scale = d.ncomp == 1;
+        for (int c = 0; c < d.ncomp; c++)
+            if (!comp_terms(p, comps[c][0], comps[c][1], &d.c[c])) {
+                *err = "derivative order too high";
+                return false;
+            }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Handle.
+// ---------------------------------------------------------------------------
+RBFFD_EXPORT int rbffd_version(void) { return RBFFD_VERSION_MAJOR * 100 + RBFFD_VERSION_MINOR; }
+
+RBFFD_EXPORT const char *rbffd_status_string(int s)
+{
+    switch (s) {
+    case RBFFD_OK: return "ok";
+    case RBFFD_EINVAL: return "invalid argument";
+    case RBFFD_ECUDA: return "CUDA error";
+    case RBFFD_ESINGULAR: return "singular local system";
+    case RBFFD_ETIMEOUT: return "device wait timed out";
+    case RBFFD_ENOMEM: return "out of memory";
+    default: return "unknown status";
+    }
+}
+
+RBFFD_EXPORT int rbffd_create(const rbffd_options *opt, rbffd_handle **out)
+{
+    if (!out) return RBFFD_EINVAL;
+    *out = nullptr;
+    rbffd_handle *h = new rbffd_handle();
+    if (opt) h->opt = *opt;
+    if (h->opt.max_refine <= 0) h->opt.max_refine = 6;
+    if (!(h->opt.refine_tol > 0)) h->opt.refine_tol = 1e-12;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= 0) {
+        g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        delete h;
+        return RBFFD_ECUDA;
+    }
+    h->device = h->opt.device;
+    if (h->device < 0 || h->device >= ndev) {
+        g_create_error = "device ordinal out of range";
+        delete h;
+        return RBFFD_EINVAL;
+    }
+    cudaDeviceProp prop;
+    if ((e = cudaSetDevice(h->device)) != cudaSuccess ||
+        (e = cudaGetDeviceProperties(&prop, h->device)) != cudaSuccess) {
+        g_create_error = std::string("cuda: ") + cudaGetErrorString(e);
+        delete h;
+        return RBFFD_ECUDA;
+    }
+    if (prop.major * 10 + prop.minor < 100) {
+        g_create_error = "librbffd is built for sm_103a (Blackwell); device is sm_" +
+                         std::to_string(prop.major) + std::to_string(prop.minor);
+        delete h;
+        return RBFFD_ECUDA;
+    }
+    h->num_sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        g_create_error = std::string("cuda: ") + cudaGetErrorString(e);
+        delete h;
+        return RBFFD_ECUDA;
+    }
+    for (auto &ev : h->ev) cudaEventCreate(&ev);
+    *out = h;
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT void rbffd_destroy(rbffd_handle *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    for (auto &ev : h->ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+RBFFD_EXPORT const char *rbffd_last_error(const rbffd_handle *h)
+{
+    if (!h) return g_create_error.c_str();
+    return h->err.c_str();
+}
+
+RBFFD_EXPORT void *rbffd_stream(rbffd_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+RBFFD_EXPORT int rbffd_synchronize(rbffd_handle *h)
+{
+    if (!h) return RBFFD_EINVAL;
+    CK(cudaStreamSynchronize(h->stream));
+    return RBFFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Operator sets.
+// ---------------------------------------------------------------------------
+static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, rbffd_opset **out,
+                       rbffd_stats *stats)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!pb || !out) return fail(h, RBFFD_EINVAL, "null argument");
+    *out = nullptr;
+    cudaSetDevice(h->device);
+    const int64_t N = pb->N;
+    if (N <= 0 || !pb->X) return fail(h, RBFFD_EINVAL, "empty node set");
+    if (N > INT32_MAX / 2) return fail(h, RBFFD_EINVAL, "too many nodes");
+    if (pb->p <= 0) return fail(h, RBFFD_EINVAL, "PHS exponent must be positive");
+    if (pb->precision != RBFFD_PREC_FP64 && pb->precision != RBFFD_PREC_MIXED)
+        return fail(h, RBFFD_EINVAL, "unknown precision mode");
+    if (pb->memspace != RBFFD_MEM_HOST && pb->memspace != RBFFD_MEM_DEVICE)
+        return fail(h, RBFFD_EINVAL, "unknown memspace");
+    bool collocated = pb->Y == nullptr || (pb->Y == pb->X && pb->M == N);
+    if (unscaled) collocated = true;
+    int64_t M = collocated ? N : pb->M;
+    if (M <= 0) return fail(h, RBFFD_EINVAL, "empty evaluation set");
+    int64_t rb = pb->row_begin, re = pb->row_end > 0 ? pb->row_end : M;
+    if (rb < 0 || rb >= re || re > M) return fail(h, RBFFD_EINVAL, "bad row range");
+    int64_t rows = re - rb;
+    int ops[RBFFD_OP_COUNT];
+    if (pb->op_mask == 0 || (pb->op_mask >> RBFFD_OP_COUNT)) return fail(h, RBFFD_EINVAL, "bad op mask");
+    int nops = ops_from_mask(pb->op_mask, ops);
+    bool needk = (pb->op_mask & (RBFFD_MASK(RBFFD_OP_DXK) | RBFFD_MASK(RBFFD_OP_DYK) | RBFFD_MASK(RBFFD_OP_HV))) != 0;
+    if (needk && (pb->k_deriv < 0 || pb->k_deriv > 10)) return fail(h, RBFFD_EINVAL, "k_deriv out of range");
+    OpTable table;
+    std::string terr;
+    if (!build_op_table(ops, nops, pb->p, pb->k_deriv, &table, &terr)) return fail(h, RBFFD_EINVAL, terr);
+
+    // stencil sizes and degrees
+    std::vector<int32_t> hn, hdeg;
+    bool uniform = !pb->n_per_node && !pb->deg_per_node;
+    int max_n = pb->n, max_deg = pb->polydeg, max_s = 0;
+    if (pb->n_per_node) {
+        if (!fetch_i32(h, pb->n_per_node, N, pb->memspace, hn)) return fail(h, RBFFD_ECUDA, "copy n_per_node");
+        max_n = *std::max_element(hn.begin(), hn.end());
+    }
+    if (pb->deg_per_node) {
+        if (!fetch_i32(h, pb->deg_per_node, N, pb->memspace, hdeg)) return fail(h, RBFFD_ECUDA, "copy deg_per_node");
+        max_deg = *std::max_element(hdeg.begin(), hdeg.end());
+    }
+    for (int64_t i = 0; i < N; i++) {
+        int n = hn.empty() ? pb->n : hn[i];
+        int d = hdeg.empty() ? pb->polydeg : hdeg[i];
+        if (n < 1 || n > N || n > RBFFD_MAX_K) return fail(h, RBFFD_EINVAL, "stencil size out of range");
+        if (d < 0 || d > RBFFD_MAX_DEG) return fail(h, RBFFD_EINVAL, "polynomial degree out of range");
+        max_s = std::max(max_s, n + npoly_h(d));
+        if (hn.empty() && hdeg.empty()) break;
+    }
+    if (max_s > RBFFD_MAX_S) return fail(h, RBFFD_EINVAL, "local system larger than 128");
+    if (pb->precision == RBFFD_PREC_MIXED && unscaled)
+        return fail(h, RBFFD_EINVAL, "the unscaled overload is FP64 only");
+
+    cudaStream_t st = h->stream;
+    Arena keep(st), tmp(st);
+    rbffd_opset *os = new rbffd_opset();
+    auto bail = [&](int code) {
+        delete os;
+        return code;
+    };
+    int rc;
+    CK(cudaEventRecord(h->ev[0], st));
+    // ---- upload
+    double2 *dX, *dY = nullptr;
+    int32_t *dcls = nullptr, *dn = nullptr, *ddeg = nullptr;
+    {
+        cudaError_t e = stage(h, keep, pb->X, (size_t)N, pb->memspace, &dX);
+        if (e == cudaSuccess && !collocated) e = stage(h, tmp, pb->Y, (size_t)M, pb->memspace, &dY);
+        if (e == cudaSuccess && pb->node_class) e = stage(h, tmp, pb->node_class, (size_t)N, pb->memspace, &dcls);
+        if (e == cudaSuccess && pb->n_per_node) e = stage(h, keep, pb->n_per_node, (size_t)N, pb->memspace, &dn);
+        if (e == cudaSuccess && pb->deg_per_node) e = stage(h, tmp, pb->deg_per_node, (size_t)N, pb->memspace, &ddeg);
+        if (e != cudaSuccess) return bail(fail(h, RBFFD_ECUDA, std::string("upload: ") + cudaGetErrorString(e)));
+    }
+    CK(cudaEventRecord(h->ev[1], st));
+    // ---- grid
+    GridBuild gb;
+    if ((rc = build_grid(h, tmp, dX, dcls, N, gb)) != RBFFD_OK) return bail(rc);
+    CK(cudaEventRecord(h->ev[2], st));
+    Flags *dflags;
+    CK(tmp.zeros(&dflags, 1));
+    {
+        int64_t big = INT64_MAX;
+        CK(cudaMemcpyAsync(&dflags->first_bad, &big, sizeof(big), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    // ---- nearest node of every row and the systems to factor
+    int32_t *nn;  // rows
+    int32_t *sys_node;
+    int64_t *sys_rows = nullptr;
+    int32_t *rows_list = nullptr;
+    int64_t nsys;
+    CK(keep.get(&nn, rows));
+    if (collocated) {
+        iota_i32<<<nblk(rows), 256, 0, st>>>(nn, rows, rb);
+        sys_node = nn;
+        nsys = rows;
+    } else {
+        // knn(tree, Y, 1): point queries, every node visible (calculateneighbors.jl:90-94)
+        CK(launch_knn(gb.g, dY + rb, nullptr, nullptr, false, rows, nullptr, 1, 1, nullptr, nn, nullptr,
+                      knn_r0(gb.rho, 1), &dflags->knn_err, h->num_sms, st));
+        int64_t *flag, *pos;
+        size_t tb = scan_tmp_bytes(N);
+        void *scratch;
+        CK(tmp.zeros(&flag, N));
+        CK(tmp.get(&pos, N + 1));
+        CK(tmp.get((char **)&scratch, tb));
+        mark_nodes<<<nblk(rows), 256, 0, st>>>(nn, rows, flag);
+        CK(scan_exclusive_i64(flag, pos, N, scratch, tb, st));
+        CK(cudaMemcpyAsync(&nsys, pos + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(tmp.get(&sys_node, nsys));
+        compact_nodes<<<nblk(N), 256, 0, st>>>(flag, pos, N, sys_node);
+        int64_t *cnt, *fill;
+        size_t tb2 = scan_tmp_bytes(nsys);
+        void *scratch2;
+        CK(tmp.zeros(&cnt, nsys + 1));
+        CK(tmp.zeros(&fill, nsys));
+        CK(tmp.get(&sys_rows, nsys + 1));
+        CK(tmp.get(&rows_list, rows));
+        CK(tmp.get((char **)&scratch2, tb2));
+        count_rows<<<nblk(rows), 256, 0, st>>>(nn, rows, pos, (unsigned long long *)cnt);
+        CK(scan_exclusive_i64(cnt, sys_rows, nsys, scratch2, tb2, st));
+        scatter_rows<<<nblk(rows), 256, 0, st>>>(nn, rows, rb, pos, sys_rows, (unsigned long long *)fill, rows_list);
+        sort_row_lists<<<nblk(nsys), 256, 0, st>>>(sys_rows, nsys, rows_list);
+    }
+    // ---- stencils: knn(tree, X, n, true) / calculateneighbors masks
+    int32_t *nbr;
+    int64_t *nbr_ptr = nullptr;
+    if (uniform) {
+        CK(keep.get(&nbr, (size_t)N * max_n));
+    } else {
+        int64_t *len;
+        size_t tb = scan_tmp_bytes(N);
+        void *scratch;
+        CK(tmp.get(&len, N));
+        CK(keep.get(&nbr_ptr, N + 1));
+        CK(tmp.get((char **)&scratch, tb));
+        if (dn) {
+            i32_to_i64<<<nblk(N), 256, 0, st>>>(dn, len, N);
+        } else {
+            // uniform n with per-node degrees
+            std::vector<int64_t> hl(N, pb->n);
+            CK(cudaMemcpyAsync(len, hl.data(), N * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        CK(scan_exclusive_i64(len, nbr_ptr, N, scratch, tb, st));
+        int64_t tot;
+        CK(cudaMemcpyAsync(&tot, nbr_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(keep.get(&nbr, tot));
+    }
+    CK(launch_knn(gb.g, dX, dcls, sys_node, true, nsys, dn, pb->n, max_n, nbr_ptr, nbr, nullptr,
+                  knn_r0(gb.rho, max_n), &dflags->knn_err, h->num_sms, st));
+    CK(cudaEventRecord(h->ev[3], st));
+    // ---- CSR row pointers
+    int64_t *row_ptr;
+    int64_t nnz;
+    CK(keep.get(&row_ptr, rows + 1));
+    if (uniform) {
+        uniform_ptr<<<nblk(rows + 1), 256, 0, st>>>(row_ptr, rows, pb->n);
+        nnz = rows * (int64_t)pb->n;
+    } else {
+        int64_t *len;
+        size_t tb = scan_tmp_bytes(rows);
+        void *scratch;
+        CK(tmp.get(&len, rows));
+        CK(tmp.get((char **)&scratch, tb));
+        row_len_kernel<<<nblk(rows), 256, 0, st>>>(nn, rows, dn, pb->n, len);
+        CK(scan_exclusive_i64(len, row_ptr, rows, scratch, tb, st));
+        CK(cudaMemcpyAsync(&nnz, row_ptr + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    int32_t *col;
+    double *val;
+    CK(keep.get(&col, nnz));
+    CK(keep.get(&val, (size_t)nnz * nops));
+    // ---- weight solves
+    SolveArgs a{};
+    a.X = dX;
+    a.Y = collocated ? nullptr : dY;
+    a.nbr = nbr;
+    a.nbr_ptr = nbr_ptr;
+    a.n_node = dn;
+    a.deg_node = ddeg;
+    a.n = pb->n;
+    a.deg = pb->polydeg;
+    a.sys_node = sys_node;
+    a.sys_rows = sys_rows;
+    a.rows_list = rows_list;
+    a.nsys = nsys;
+    a.row_begin = rb;
+    a.row_ptr = row_ptr;
+    a.col = col;
+    a.val = val;
+    a.nnz = nnz;
+    a.max_s = max_s;
+    a.max_n = max_n;
+    a.first_bad = &dflags->first_bad;
+    a.max_refine = h->opt.max_refine;
+    a.refine_tol = h->opt.refine_tol;
+    a.unscaled_overload = unscaled;
+    int32_t *fb_list = nullptr;
+    if (pb->precision == RBFFD_PREC_MIXED) {
+        CK(tmp.get(&fb_list, nsys));
+        a.fallback_list = fb_list;
+        a.fallback_count = &dflags->fallback_count;
+        a.hist = dflags->hist;
+        int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(max_s, max_n, nops));
+        CK(launch_solve_mixed(a, table, wpb, h->num_sms, st));
+    } else {
+        int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
+        CK(launch_solve_fp64(a, table, wpb, h->num_sms, st));
+    }
+    CK(cudaEventRecord(h->ev[4], st));
+    Flags hf;
+    CK(cudaMemcpyAsync(&hf, dflags, sizeof(Flags), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (pb->precision == RBFFD_PREC_MIXED && hf.fallback_count > 0 && !hf.knn_err) {
+        int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
+        CK(launch_solve_fp64_subset(a, table, wpb, h->num_sms, st, hf.fallback_count));
+        CK(cudaMemcpyAsync(&hf.first_bad, &dflags->first_bad, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaEventRecord(h->ev[5], st));
+    CK(cudaStreamSynchronize(st));
+    if (hf.knn_err) return bail(fail(h, RBFFD_EINVAL, "fewer candidate nodes than the stencil size"));
+    if (hf.first_bad != INT64_MAX) {
+        if (stats) stats->first_bad_node = hf.first_bad;
+        return bail(fail(h, RBFFD_ESINGULAR, "singular local system at node " + std::to_string(hf.first_bad)));
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->ms_upload = elapsed(h->ev[0], h->ev[1]);
+        stats->ms_grid = elapsed(h->ev[1], h->ev[2]);
+        stats->ms_knn = elapsed(h->ev[2], h->ev[3]);
+        stats->ms_solve = elapsed(h->ev[3], h->ev[4]);
+        stats->ms_fallback = elapsed(h->ev[4], h->ev[5]);
+        stats->ms_total = elapsed(h->ev[0], h->ev[5]);
+        stats->n_systems = nsys;
+        stats->n_rows = rows;
+        stats->n_fallback = pb->precision == RBFFD_PREC_MIXED ? hf.fallback_count : 0;
+        stats->first_bad_node = -1;
+        for (int i = 0; i < 8; i++) stats->refine_hist[i] = (int64_t)hf.hist[i];
+        stats->nnz = nnz;
+        // kernels launched: grid (bbox 2, fill 1, scan 3, scatter/narrow/cell sort 3), row
+        // grouping, stencil offsets, kNN, row pointers, solve (+ FP64 fallback)
+        int64_t nk = 9;
+        nk += collocated ? 1 : 12;
+        if (!uniform) nk += (dn ? 1 : 0) + 3;
+        nk += 1;
+        nk += uniform ? 1 : 4;
+        nk += 1;
+        if (pb->precision == RBFFD_PREC_MIXED && hf.fallback_count > 0) nk += 1;
+        stats->kernel_launches = nk;
+    }
+    os->N = N;
+    os->M = M;
+    os->rows = rows;
+    os->row_begin = rb;
+    os->nnz = nnz;
+    os->nops = nops;
+    memcpy(os->ops, ops, sizeof(int) * nops);
+    os->collocated = collocated;
+    os->uniform = uniform;
+    os->n = pb->n;
+    os->X = dX;
+    os->nbr = nbr;
+    os->nbr_ptr = nbr_ptr;
+    os->nn = nn;
+    os->row_ptr = row_ptr;
+    os->col = col;
+    os->val = val;
+    keep.release_to(os->owned);
+    *out = os;
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_opset_create(rbffd_handle *h, const rbffd_problem *pb, rbffd_opset **out,
+                                    rbffd_stats *stats)
+{
+    return opset_build(h, pb, 0, out, stats);
+}
+
+RBFFD_EXPORT void rbffd_opset_destroy(rbffd_handle *h, rbffd_opset *s)
+{
+    if (!s) return;
+    if (h) {
+        cudaSetDevice(h->device);
+        for (void *p : s->owned) cudaFreeAsync(p, h->stream);
+        cudaStreamSynchronize(h->stream);
+    } else {
+        for (void *p : s->owned) cudaFree(p);
+    }
+    delete s;
+}
+
+RBFFD_EXPORT int rbffd_opset_shape(const rbffd_opset *s, int64_t *rows, int64_t *cols, int64_t *nnz, int *nops)
+{
+    if (!s) return RBFFD_EINVAL;
+    if (rows) *rows = s->rows;
+    if (cols) *cols = s->N;
+    if (nnz) *nnz = s->nnz;
+    if (nops) *nops = s->nops;
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_opset_device_csr(const rbffd_opset *s, int op, const int64_t **row_ptr,
+                                        const int32_t **col, const double **val)
+{
+    if (!s || op < 0 || op >= s->nops) return RBFFD_EINVAL;
+    if (row_ptr) *row_ptr = s->row_ptr;
+    if (col) *col = s->col;
+    if (val) *val = s->val + (size_t)op * s->nnz;
+    return RBFFD_OK;
+}
+
+static int ensure_csc(rbffd_handle *h, rbffd_opset *s)
+{
+    if (s->csc_perm) return RBFFD_OK;
+    cudaStream_t st = h->stream;
+    Arena keep(st), tmp(st);
+    int64_t N = s->N;
+    int64_t *count, *colstart, *fill, *rowval, *perm;
+    double *buf;
+    size_t tb = scan_tmp_bytes(N);
+    void *scratch;
+    CK(tmp.zeros(&count, N + 1));
+    CK(keep.get(&colstart, N + 1));
+    CK(tmp.zeros(&fill, N));
+    CK(keep.get(&rowval, s->nnz));
+    CK(keep.get(&perm, s->nnz));
+    CK(keep.get(&buf, s->nnz));
+    CK(tmp.get((char **)&scratch, tb));
+    CK(launch_csc_count(s->nnz, s->col, count, st));
+    CK(scan_exclusive_i64(count, colstart, N, scratch, tb, st));
+    CK(launch_csc_scatter(s->rows, s->row_ptr, s->col, s->row_begin, colstart, fill, rowval, perm, st));
+    CK(launch_csc_sort_segments(N, colstart, rowval, perm, st));
+    // Julia is 1-based
+    CK(launch_add_i64(N + 1, colstart, 1, st));
+    CK(launch_add_i64(s->nnz, rowval, 1, st));
+    CK(cudaStreamSynchronize(st));
+    s->csc_colptr = colstart;
+    s->csc_rowval = rowval;
+    s->csc_perm = perm;
+    s->csc_tmp = buf;
+    keep.release_to(s->owned);
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_opset_export_csc(rbffd_handle *h, rbffd_opset *s, int op, rbffd_csc *out)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || !out || op < 0 || op >= s->nops) return fail(h, RBFFD_EINVAL, "bad export arguments");
+    cudaSetDevice(h->device);
+    int rc = ensure_csc(h, s);
+    if (rc) return rc;
+    cudaStream_t st = h->stream;
+    CK(launch_gather_f64(s->nnz, s->csc_perm, s->val + (size_t)op * s->nnz, s->csc_tmp, st));
+    if (out->colptr)
+        CK(cudaMemcpyAsync(out->colptr, s->csc_colptr, (s->N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    if (out->rowval)
+        CK(cudaMemcpyAsync(out->rowval, s->csc_rowval, s->nnz * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    if (out->nzval)
+        CK(cudaMemcpyAsync(out->nzval, s->csc_tmp, s->nnz * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_opset_export_csr(rbffd_handle *h, rbffd_opset *s, int op, int64_t *row_ptr,
+                                        int32_t *col, double *val)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || op < 0 || op >= s->nops) return fail(h, RBFFD_EINVAL, "bad export arguments");
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    if (row_ptr) CK(cudaMemcpyAsync(row_ptr, s->row_ptr, (s->rows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    if (col) CK(cudaMemcpyAsync(col, s->col, s->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    if (val)
+        CK(cudaMemcpyAsync(val, s->val + (size_t)op * s->nnz, s->nnz * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_opset_export_stencils(rbffd_handle *h, rbffd_opset *s, int32_t *nbr, int32_t *nn)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s) return fail(h, RBFFD_EINVAL, "null set");
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    if (nbr) {
+        if (!s->uniform) return fail(h, RBFFD_EINVAL, "stencil export needs a uniform stencil size");
+        CK(cudaMemcpyAsync(nbr, s->nbr, (size_t)s->N * s->n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    }
+    if (nn) CK(cudaMemcpyAsync(nn, s->nn, s->rows * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_spmv(rbffd_handle *h, rbffd_opset *s, int op, const double *x, double *y)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || op < 0 || op >= s->nops || !x || !y) return fail(h, RBFFD_EINVAL, "bad spmv arguments");
+    double avg = s->rows > 0 ? (double)s->nnz / s->rows : 0;
+    int group = avg >= 24 ? 32 : (avg >= 12 ? 16 : 8);
+    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, group, h->num_sms,
+                       h->stream));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, int nfields,
+                            int dtype)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || op < 0 || op >= s->nops || !x || !y || nfields <= 0 || (dtype != 0 && dtype != 1))
+        return fail(h, RBFFD_EINVAL, "bad spmm arguments");
+    const void *v = s->val + (size_t)op * s->nnz;
+    if (dtype == 1) {
+        if (!s->val32) {
+            float *v32;
+            CK(cudaMallocAsync((void **)&v32, (size_t)s->nnz * s->nops * sizeof(float), h->stream));
+            s->owned.push_back(v32);
+            CK(launch_f64_to_f32((int64_t)s->nnz * s->nops, s->val, v32, h->stream));
+            s->val32 = v32;
+        }
+        v = s->val32 + (size_t)op * s->nnz;
+    }
+    CK(launch_spmm(s->rows, s->row_ptr, s->col, v, x, y, nfields, dtype, h->stream));
+    return RBFFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in entry points.
+// ---------------------------------------------------------------------------
+static int export_all(rbffd_handle *h, rbffd_opset *s, rbffd_csc *out)
+{
+    for (int q = 0; q < s->nops; q++) {
+        int rc = rbffd_opset_export_csc(h, s, q, &out[q]);
+        if (rc) return rc;
+    }
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_generate_operator(rbffd_handle *h, const double *X, int64_t N, const double *Y,
+                                         int64_t M, int p, int n, int polydeg, const int32_t *node_class,
+                                         uint32_t op_mask, int precision, rbffd_csc *out,
+                                         rbffd_stats *stats)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!out) return fail(h, RBFFD_EINVAL, "null output");
+    rbffd_problem pb{};
+    pb.X = X;
+    pb.N = N;
+    pb.Y = Y;
+    pb.M = M;
+    pb.p = p;
+    pb.n = n;
+    pb.polydeg = polydeg;
+    pb.node_class = node_class;
+    pb.op_mask = op_mask;
+    pb.precision = precision;
+    pb.memspace = RBFFD_MEM_HOST;
+    rbffd_opset *s = nullptr;
+    int rc = opset_build(h, &pb, 0, &s, stats);
+    if (rc) return rc;
+    rc = export_all(h, s, out);
+    rbffd_opset_destroy(h, s);
+    return rc;
+}
+
+RBFFD_EXPORT int rbffd_hyperviscosity_operator(rbffd_handle *h, int k_deriv, const double *X, int64_t N,
+                                               const double *Y, int64_t M, int p, int n, int polydeg,
+                                               const int32_t *node_class, int precision, rbffd_csc *out,
+                                               rbffd_stats *stats)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!out) return fail(h, RBFFD_EINVAL, "null output");
+    rbffd_problem pb{};
+    pb.X = X;
+    pb.N = N;
+    pb.Y = Y;
+    pb.M = M;
+    pb.p = p;
+    pb.n = n;
+    pb.polydeg = polydeg;
+    pb.node_class = node_class;
+    pb.op_mask = RBFFD_MASK_HYPERVISCOSITY;
+    pb.k_deriv = k_deriv;
+    pb.precision = precision;
+    pb.memspace = RBFFD_MEM_HOST;
+    rbffd_opset *s = nullptr;
+    int rc = opset_build(h, &pb, 0, &s, stats);
+    if (rc) return rc;
+    rc = export_all(h, s, out);
+    rbffd_opset_destroy(h, s);
+    return rc;
+}
+
+RBFFD_EXPORT int rbffd_generate_operator_unscaled(rbffd_handle *h, const double *X, int64_t N, int p, int n,
+                                                  int polydeg, uint32_t op_mask, int k_deriv, rbffd_csc *out,
+                                                  rbffd_stats *stats)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!out) return fail(h, RBFFD_EINVAL, "null output");
+    rbffd_problem pb{};
+    pb.X = X;
+    pb.N = N;
+    pb.p = p;
+    pb.n = n;
+    pb.polydeg = polydeg;
+    pb.op_mask = op_mask;
+    pb.k_deriv = k_deriv;
+    pb.precision = RBFFD_PREC_FP64;
+    pb.memspace = RBFFD_MEM_HOST;
+    rbffd_opset *s = nullptr;
+    int rc = opset_build(h, &pb, 1, &s, stats);
+    if (rc) return rc;
+    rc = export_all(h, s, out);
+    rbffd_opset_destroy(h, s);
+    return rc;
+}
+
+RBFFD_EXPORT int rbffd_calculateneighbors(rbffd_handle *h, const double *X, int64_t N, const double *Y,
+                                          int64_t M, int n, const int32_t *node_class, int64_t *idxs_x,
+                                          double *dists_x, int64_t *idxs_y_x, double *dists_y_x)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!X || N <= 0 || n < 1 || n > N || n > RBFFD_MAX_K || !idxs_x || M < 0 || (M > 0 && (!Y || !idxs_y_x)))
+        return fail(h, RBFFD_EINVAL, "bad calculateneighbors arguments");
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    Arena tmp(st);
+    double2 *dX, *dY = nullptr;
+    int32_t *dcls = nullptr;
+    CK(stage(h, tmp, X, (size_t)N, RBFFD_MEM_HOST, &dX));
+    if (M > 0) CK(stage(h, tmp, Y, (size_t)M, RBFFD_MEM_HOST, &dY));
+    if (node_class) CK(stage(h, tmp, node_class, (size_t)N, RBFFD_MEM_HOST, &dcls));
+    GridBuild gb;
+    int rc = build_grid(h, tmp, dX, dcls, N, gb);
+    if (rc) return rc;
+    int *err;
+    int32_t *idx;
+    double *d2;
+    int64_t *oidx;
+    double *od;
+    int64_t tot = N * (int64_t)n, big = std::max<int64_t>(tot, M);
+    CK(tmp.zeros(&err, 1));
+    CK(tmp.get(&idx, big));
+    CK(tmp.get(&d2, big));
+    CK(tmp.get(&oidx, big));
+    CK(tmp.get(&od, big));
+    CK(launch_knn(gb.g, dX, dcls, nullptr, true, N, nullptr, n, n, nullptr, idx, d2, knn_r0(gb.rho, n), err,
+                  h->num_sms, st));
+    knn_export<<<nblk(tot), 256, 0, st>>>(idx, d2, tot, oidx, od);
+    CK(cudaMemcpyAsync(idxs_x, oidx, tot * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    if (dists_x) CK(cudaMemcpyAsync(dists_x, od, tot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (M > 0) {
+        CK(launch_knn(gb.g, dY, nullptr, nullptr, false, M, nullptr, 1, 1, nullptr, idx, d2, knn_r0(gb.rho, 1), err,
+                      h->num_sms, st));
+        knn_export<<<nblk(M), 256, 0, st>>>(idx, d2, M, oidx, od);
+        CK(cudaMemcpyAsync(idxs_y_x, oidx, M * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        if (dists_y_x) CK(cudaMemcpyAsync(dists_y_x, od, M * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (herr) return fail(h, RBFFD_EINVAL, "fewer candidate nodes than the stencil size");
+    return RBFFD_OK;
+}

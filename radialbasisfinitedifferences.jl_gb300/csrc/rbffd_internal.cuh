@@ -1,0 +1,160 @@
+// Internal declarations shared by the CUDA translation units of librbffd.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "rbffd.h"
+
+#define RBFFD_FULL 0xffffffffu
+#define RBFFD_MAX_OPS 10
+#define RBFFD_MAX_TERMS 6
+#define RBFFD_MAX_S 128   // largest local system (n + m) the solve kernels accept
+#define RBFFD_MAX_K 128   // largest stencil size the kNN kernel accepts
+#define RBFFD_MAX_DEG 8   // largest polynomial degree
+
+// ---------------------------------------------------------------------------
+// Operator descriptors (host-built, passed by value to the solve kernels).
+//   Each operator is one or two derivative components (a, b) = d^a/dx^a d^b/dy^b.
+//   The RBF part of component c is sum_t coef * x^ex * y^ey * r^er (closed form of
+//   d^a/dx^a d^b/dy^b r^p).  Single-component operators are unscaled after the solve
+//   by sx^a sy^b (src/generate_operator.jl:161-166); two-component operators (LAP, HV)
+//   scale each component by sx^a sy^b inside the right-hand side.
+// ---------------------------------------------------------------------------
+struct RbfTerm {
+    double coef;
+    int ex, ey, er;
+};
+
+struct OpComp {
+    int a, b;  // derivative orders
+    int nterm;
+    RbfTerm t[RBFFD_MAX_TERMS];
+};
+
+struct OpDesc {
+    int ncomp;       // 1 or 2
+    int post_scale;  // 1: multiply weights by sx^a sy^b after the solve
+    OpComp c[2];
+};
+
+struct OpTable {
+    int nops;
+    int p;
+    OpDesc op[RBFFD_MAX_OPS];
+};
+
+// Build the descriptor table for the ops in `ops` (RBFFD_OP_* codes).
+bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, std::string *err);
+
+// ---------------------------------------------------------------------------
+// Device scratch helpers.
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Uniform grid of cells over the node set (kNN candidate lookup).
+// ---------------------------------------------------------------------------
+struct GridDev {
+    double x0, y0, cs;
+    int nx, ny;
+    const int32_t *start;  // nx*ny + 1 offsets into pts/ids/cls
+    const double2 *pts;    // node coordinates in cell order
+    const int32_t *ids;    // node ids in cell order
+    const int32_t *cls;    // node classes in cell order (nullable)
+};
+
+// ---------------------------------------------------------------------------
+// Launch wrappers implemented in the .cu files.  All run on `st` and return a
+// cudaError_t of the launch; device-side failures are reported through flag words.
+// ---------------------------------------------------------------------------
+
+// exclusive scan of n int64 values (in place allowed), out has n+1 entries (out[n] = total).
+cudaError_t scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, void *tmp,
+                               size_t tmp_bytes, cudaStream_t st);
+size_t scan_tmp_bytes(int64_t n);
+
+// bounding box of N points: out[0..3] = xmin, xmax, ymin, ymax; out_bad[0] = #non-finite.
+cudaError_t launch_bbox(const double2 *X, int64_t N, double *partial, int nblocks, double *out,
+                        int *out_bad, cudaStream_t st);
+
+cudaError_t launch_grid_fill(const double2 *X, const int32_t *cls, int64_t N, double x0,
+                             double y0, double cs, int nx, int ny, int64_t *cell_count,
+                             int32_t *cell_of, cudaStream_t st);
+cudaError_t launch_grid_scatter(const double2 *X, const int32_t *cls, int64_t N,
+                                const int32_t *cell_of, const int64_t *cell_start64,
+                                int32_t *cell_start32, int64_t ncell, int32_t *fill,
+                                double2 *pts, int32_t *ids, int32_t *gcls, cudaStream_t st);
+
+// kNN: for each query its k nearest grid nodes allowed by the class mask, sorted by
+// (d^2, id).  Node queries (node_query): query q is node q_node[q] (or q) with coordinates
+// Q[node], class qcls[node], size kq[node] (or kuni), output at out_ptr[node] (or node*k).
+// Point queries: coordinates Q[q], class 0 (sees every node), size kuni, output at q*kuni.
+cudaError_t launch_knn(const GridDev &g, const double2 *Q, const int32_t *qcls,
+                       const int32_t *q_node, bool node_query, int64_t nq,
+                       const int32_t *kq, int kuni, int kmax, const int64_t *out_ptr,
+                       int32_t *out_idx, double *out_d2, int r0, int *err_flag,
+                       int num_sms, cudaStream_t st);
+
+// Weight solves.
+struct SolveArgs {
+    const double2 *X;
+    const double2 *Y;          // nullable: collocated (row y <-> node y)
+    const int32_t *nbr;        // stencils
+    const int64_t *nbr_ptr;    // nullable: uniform stencils of length n
+    const int32_t *n_node;     // nullable per-node stencil size
+    const int32_t *deg_node;   // nullable per-node degree
+    int n, deg;                // uniform values
+    const int32_t *sys_node;   // nsys X nodes to factor
+    const int64_t *sys_rows;   // nullable: rows of system i are rows_list[sys_rows[i]..sys_rows[i+1])
+    const int32_t *rows_list;  // row ids (global evaluation-point ids)
+    int64_t nsys;
+    int64_t row_begin;         // rows are stored at (row - row_begin)
+    const int64_t *row_ptr;    // local row -> offset in col/val
+    int32_t *col;              // nnz
+    double *val;               // nops * nnz (op-major)
+    int64_t nnz;
+    int max_s, max_n;          // largest s / n over the systems (smem sizing)
+    int64_t *first_bad;        // atomicMin of failing node (init INT64_MAX)
+    int32_t *fallback_list;    // mixed: systems needing FP64 (nullable for plain)
+    int *fallback_count;
+    unsigned long long *hist;  // mixed: refinement histogram [8]
+    int max_refine;
+    double refine_tol;
+    int unscaled_overload;     // generate_operator(X,p,n,polydeg) quirk
+};
+
+cudaError_t launch_solve_fp64(const SolveArgs &a, const OpTable &ops, int warps_per_block,
+                              int num_sms, cudaStream_t st);
+cudaError_t launch_solve_mixed(const SolveArgs &a, const OpTable &ops, int warps_per_block,
+                               int num_sms, cudaStream_t st);
+// FP64 re-solve of the systems the mixed kernel queued in a.fallback_list.
+cudaError_t launch_solve_fp64_subset(const SolveArgs &a, const OpTable &ops, int warps_per_block,
+                                     int num_sms, cudaStream_t st, int64_t count);
+size_t solve_fp64_smem_per_warp(int max_s, int max_n, int nops);
+size_t solve_mixed_smem_per_warp(int max_s, int max_n, int nops);
+
+// Sparse kernels.
+cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t *col,
+                            const double *val, const double *x, double *y, int group,
+                            int num_sms, cudaStream_t st);
+cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col,
+                        const void *val, const void *x, void *y, int nfields, int dtype,
+                        cudaStream_t st);
+cudaError_t launch_csc_count(int64_t nnz, const int32_t *col, int64_t *colcount,
+                             cudaStream_t st);
+cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32_t *col,
+                               int64_t row_begin, const int64_t *colstart, int64_t *fill,
+                               int64_t *rowval, int64_t *perm, cudaStream_t st);
+cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int64_t *rowval,
+                                     int64_t *perm, cudaStream_t st);
+cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *src, double *dst,
+                              cudaStream_t st);
+cudaError_t launch_add_i64(int64_t n, int64_t *a, int64_t v, cudaStream_t st);
+cudaError_t launch_f64_to_f32(int64_t n, const double *a, float *b, cudaStream_t st);

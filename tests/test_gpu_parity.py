@@ -1,0 +1,277 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the CPU oracle.
+
+Bars: kNN indices bit-exact; FP64 weights within 1e-10 row-relative (max over rows of
+||w - w_oracle||_inf / ||w_oracle||_inf; the oracle inverts A explicitly as the reference
+does, the GPU solves with LU factors, both in FP64, and the local systems here have
+cond(A) <= ~1e6, so rounding differences stay far below this); mixed precision within
+1e-9, the bar the reference's Float64 weights are held to; sparse structure identical.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+from conftest import rel_row_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-9
+ALL6 = ("E", "Dx", "Dy", "Dxx", "Dyy", "Dxy")
+
+
+def grid(pkg, nx, seed=1):
+    X, h, _ = pkg.nodesets.jittered_grid(nx, seed=seed)
+    return X, h
+
+
+def test_knn_bit_exact(pkg, orc, gpu):
+    X, _ = grid(pkg, 64)
+    for n in (1, 15, 30, 45, 64, 90):
+        ix, iy, dx, dy = pkg.calculateneighbors(X, X[:100] + 1e-3, n)
+        ref, d2 = orc.knn(X, X, n)
+        assert (ix - 1 == ref).all(), n
+        assert np.array_equal(dx, np.sqrt(d2))
+        refy, _ = orc.knn(X, X[:100] + 1e-3, 1)
+        assert (iy - 1 == refy).all()
+
+
+def test_knn_boundary_mask(pkg, orc, gpu):
+    d = pkg.nodesets.rectangle_with_ghosts(total=6000, seed=3)
+    X, cls = d["X"], d["node_class"]
+    n = 20
+    ids = np.arange(1, len(X) + 1)
+    rin = ids[cls == 0]
+    rbc = [ids[cls == b] for b in range(1, 5)]
+    rg = [ids[cls == -b] for b in range(1, 5)]
+    ix, iy, _, _ = pkg.calculateneighbors(X, X[:50], n, rin, rbc, rg)
+    ref, _ = orc.knn(X, X, n, cls_x=cls, cls_q=cls)
+    assert (ix - 1 == ref).all()
+    # a boundary node of b never sees ghosts of other boundaries (calculateneighbors.jl:23-30)
+    for b in range(1, 5):
+        sel = ix[cls == b] - 1
+        c = cls[sel]
+        assert ((c >= 0) | (c == -b)).all()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_weights_all_ops(pkg, orc, gpu, precision, tol):
+    X, _ = grid(pkg, 64)
+    p, n, deg = 3, 15, 2
+    ops = ALL6 + ("Lap",)
+    ref = orc.generate(X, X, p, n, deg, ops)
+    with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision=precision) as s:
+        for q, o in enumerate(s.ops):
+            rp, col, val = s.csr_arrays(o)
+            assert (col.reshape(-1, n) == ref["cols"]).all()
+            assert rel_row_err(val, ref["W"][ops.index(o)]) < tol, o
+
+
+@pytest.mark.parametrize("cfg", [(3, 30, 3), (3, 20, 2), (5, 42, 5), (3, 45, 4), (3, 60, 5)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_weights_sizes(pkg, orc, gpu, cfg, precision):
+    p, n, deg = cfg
+    X, _ = grid(pkg, 48, seed=5)
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision=precision) as s:
+        for o in s.ops:
+            _, col, val = s.csr_arrays(o)
+            assert (col.reshape(-1, n) == ref["cols"]).all()
+            assert rel_row_err(val, ref["W"][ops.index(o)]) < (FP64_TOL if precision == "fp64" else MIXED_TOL), o
+
+
+def test_hyperviscosity_weights(pkg, orc, gpu):
+    X, _ = grid(pkg, 48, seed=6)
+    p, n, deg, K = 5, 30, 3, 4
+    ops = ("Dxk", "Dyk", "HV")
+    ref = orc.generate(X, X, p, n, deg, ops, k_deriv=K)
+    with pkg.OperatorSet(X, None, p, n, deg, ops=ops, k_deriv=K, precision="fp64") as s:
+        for o in s.ops:
+            assert rel_row_err(s.csr_arrays(o)[2], ref["W"][ops.index(o)]) < FP64_TOL, o
+
+
+def test_generate_operator_csc_matches_sparse(pkg, orc, gpu):
+    """The Julia-layout CSC equals sparse(I, J, V) of the oracle: same colptr/rowval, values."""
+    X, _ = grid(pkg, 40, seed=2)
+    Y = X[::3] + 1e-4  # non-collocated
+    p, n, deg = 3, 20, 3
+    mats = pkg.generate_operator(X, Y, p, n, deg)
+    ref = orc.generate(X, Y, p, n, deg, ALL6)
+    for q, A in enumerate(mats):
+        cp, rv, nz = orc.to_csc(len(Y), len(X), ref["cols"], ref["W"][q])
+        assert np.array_equal(A.indptr, cp - 1)
+        assert np.array_equal(A.indices, rv - 1)
+        scale = np.abs(ref["W"][q]).max()
+        assert np.abs(A.data - nz).max() <= FP64_TOL * scale * 10
+
+
+def test_unscaled_overload(pkg, orc, gpu):
+    X, _ = grid(pkg, 32, seed=8)
+    p, n, deg = 3, 15, 2
+    mats = pkg.generate_operator(X, p, n, deg)
+    ref = orc.generate_unscaled(X, p, n, deg, ALL6)
+    for q, A in enumerate(mats):
+        R = orc.to_csc(len(X), len(X), ref["cols"], ref["W"][q])
+        W = A.toarray()
+        Wr = np.zeros_like(W)
+        rows = np.repeat(np.arange(len(X)), n)
+        Wr[rows, ref["cols"].ravel()] = ref["W"][q].ravel()
+        err = (np.abs(W - Wr).max(1) / np.abs(Wr).max(1)).max()
+        assert err < 1e-8, (ALL6[q], err)  # unscaled local systems are worse conditioned
+        assert np.array_equal(A.indptr, R[0] - 1)
+    dxk, dyk = pkg.hyperviscosity_operator(2, X, p, n, deg)
+    refk = orc.generate_unscaled(X, p, n, deg, ("Dxk", "Dyk"), k_deriv=2)
+    Wr = np.zeros((len(X), len(X)))
+    Wr[np.repeat(np.arange(len(X)), n), refk["cols"].ravel()] = refk["W"][0].ravel()
+    assert (np.abs(dxk.toarray() - Wr).max(1) / np.abs(Wr).max(1)).max() < 1e-8
+
+
+def test_poisson_reference_test(pkg, orc, gpu, tominec):
+    """test/poisson_test.jl: Tominec's fitted nodes, p=3, deg 3, n=20, Y != X: err < 0.0027."""
+    X = tominec["x_nodes"]
+    Y = tominec["y_nodes"].copy()
+    idx, _ = orc.knn(Y, X, 1)
+    Y[idx[:, 0]] = X
+    E, Dx, Dy, Dxx, Dyy, Dxy = pkg.generate_operator(X, Y, 3, 20, 3)
+    err = poisson_error(X, Y, E, Dx, Dy, Dxx, Dyy, tominec, orc)
+    assert err < 0.0027, err
+
+
+def poisson_error(X, Y, E, Dx, Dy, Dxx, Dyy, t, orc):
+    M, N = len(Y), len(X)
+    ii = t["y_idx_in"] - 1
+    idr = t["y_idx_dirichlet"] - 1
+    ine = t["y_idx_neumann"] - 1
+    nx, ny = t["x_normals"][:, 2], t["y_normals"][:, 2]
+    E, Dx, Dy, Dxx, Dyy = (A.toarray() for A in (E, Dx, Dy, Dxx, Dyy))
+    D = np.zeros((M, N))
+    D[ii] = Dxx[ii] + Dyy[ii]
+    D[ine] = nx[:, None] * Dx[ine] + ny[:, None] * Dy[ine]
+    D[idr] = E[idr]
+    ue = lambda x, y: np.sin(2 * np.pi * x * y)  # noqa: E731
+    f = np.zeros(M)
+    x, y = Y[:, 0], Y[:, 1]
+    f[ii] = x[ii] ** 2 * np.pi**2 * np.sin(x[ii] * y[ii] * np.pi * 2.0) * (-4.0) - y[ii] ** 2 * np.pi**2 * np.sin(
+        x[ii] * y[ii] * np.pi * 2.0
+    ) * 4.0
+    f[ine] = ny * x[ine] * np.pi * np.cos(x[ine] * y[ine] * np.pi * 2.0) * 2.0 + nx * y[ine] * np.pi * np.cos(
+        x[ine] * y[ine] * np.pi * 2.0
+    ) * 2.0
+    f[idr] = ue(x[idr], y[idr])
+    _, d2 = orc.knn(X, X, 2)
+    h = np.mean(np.sqrt(d2[:, 1]))
+    for idx, c in ((ii, 1 / np.sqrt(len(ii))), (ine, 1 / np.sqrt(len(ine))), (idr, 1 / h / np.sqrt(len(idr)))):
+        D[idx] *= c
+        f[idx] *= c
+    u = sl.lstsq(D, f, lapack_driver="gelsy")[0]
+    uY = E @ u
+    return np.linalg.norm(uY - ue(x, y)) / np.linalg.norm(ue(x, y))
+
+
+def test_hyperviscosity_reference_test(pkg, gpu, tominec):
+    """test/hyperviscosity_test.jl: p=5, deg 5, n=42 on Tominec's nodes: Dxk ~ Dxx, Dyk ~ Dyy."""
+    X = tominec["x_nodes"]
+    E, Dx, Dy, Dxx, Dyy, Dxy = pkg.generate_operator(X, X, 5, 42, 5)
+    Dxk, Dyk = pkg.hyperviscosity_operator(2, X, X, 5, 42, 5)
+    rtol = np.sqrt(np.finfo(float).eps)
+    for A, B in ((Dxk, Dxx), (Dyk, Dyy)):
+        assert np.linalg.norm((A - B).toarray()) <= rtol * max(np.linalg.norm(A.toarray()), np.linalg.norm(B.toarray()))
+
+
+def test_boundary_aware_generate(pkg, orc, gpu):
+    d = pkg.nodesets.rectangle_with_ghosts(total=5000, seed=11)
+    X, cls = d["X"], d["node_class"]
+    ids = np.arange(1, len(X) + 1)
+    rin, rbc, rg = ids[cls == 0], [ids[cls == b] for b in range(1, 5)], [ids[cls == -b] for b in range(1, 5)]
+    p, n, deg = 3, 20, 2
+    mats = pkg.generate_operator(X, X, p, n, deg, rin, rbc, rg, rin, rbc, rg)
+    ref = orc.generate(X, X, p, n, deg, ALL6, cls=cls)
+    for q, A in enumerate(mats):
+        Wr = np.zeros((len(X), len(X)))
+        Wr[np.repeat(np.arange(len(X)), n), ref["cols"].ravel()] = ref["W"][q].ravel()
+        W = A.toarray()
+        assert (np.abs(W - Wr).max(1) / np.abs(Wr).max(1)).max() < FP64_TOL, ALL6[q]
+
+
+def test_uneven_batch(pkg, orc, gpu):
+    d = pkg.nodesets.rectangle_with_ghosts(total=8000, seed=12, main_fraction=0.5)
+    X, cls, nn, dd = d["X"], d["node_class"], d["n"], d["deg"]
+    ops = ("Dx", "Dy", "Lap")
+    # oracle per size class: evaluation points X[rows] are the nodes themselves, so each row
+    # uses its own node's stencil (with its boundary class) and its own (k, deg)
+    refs = {}
+    for k, g in pkg.nodesets.SIZE_CLASSES:
+        rows = np.nonzero((nn == k) & (dd == g))[0]
+        refs[(k, g)] = (rows, orc.generate(X, X[rows], 3, k, g, ops, cls=cls))
+    for precision, tol in (("fp64", FP64_TOL), ("mixed", MIXED_TOL)):
+        with pkg.OperatorSet(X, None, 3, 0, 0, ops=ops, precision=precision, node_class=cls, n_per_node=nn,
+                             deg_per_node=dd) as s:
+            for q, o in enumerate(ops):
+                rp, col, val = s.csr_arrays(o)
+                for (k, g), (rows, ref) in refs.items():
+                    W = np.stack([val[rp[r]:rp[r + 1]] for r in rows])
+                    C = np.stack([col[rp[r]:rp[r + 1]] for r in rows])
+                    assert (C == ref["cols"]).all()
+                    assert rel_row_err(W, ref["W"][q]) < tol, (precision, o, k)
+
+
+def test_spmv_and_spmm(pkg, orc, gpu):
+    import torch
+
+    X, _ = grid(pkg, 64, seed=3)
+    p, n, deg = 3, 15, 2
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(len(X))
+    with pkg.OperatorSet(X, None, p, n, deg, ops=ops) as s:
+        xd = torch.tensor(x, device="cuda")
+        yd = torch.empty_like(xd)
+        for q, o in enumerate(ops):
+            s.spmv(o, xd, yd)
+            yr = orc.spmv_rows(ref["cols"], ref["W"][q], x)
+            assert np.abs(yd.cpu().numpy() - yr).max() <= 1e-10 * np.abs(yr).max()
+        F = 40
+        Xf = rng.standard_normal((len(X), F))
+        xf = torch.tensor(Xf, device="cuda")
+        yf = torch.empty_like(xf)
+        s.spmm("Lap", xf, yf)
+        yr = np.stack([orc.spmv_rows(ref["cols"], ref["W"][2], Xf[:, f]) for f in range(F)], 1)
+        assert np.abs(yf.cpu().numpy() - yr).max() <= 1e-10 * np.abs(yr).max()
+        x32 = xf.float()
+        y32 = torch.empty_like(x32)
+        s.spmm("Lap", x32, y32)
+        assert np.abs(y32.cpu().numpy() - yr).max() <= 1e-4 * np.abs(yr).max()
+
+
+def test_row_range_shards(pkg, orc, gpu):
+    X, _ = grid(pkg, 40, seed=4)
+    p, n, deg = 3, 20, 3
+    full = orc.generate(X, X, p, n, deg, ("Lap",))
+    N = len(X)
+    cuts = [0, 517, 1100, N]
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        with pkg.OperatorSet(X, None, p, n, deg, ops=("Lap",), row_range=(a, b)) as s:
+            _, col, val = s.csr_arrays("Lap")
+            assert (col.reshape(-1, n) == full["cols"][a:b]).all()
+            assert rel_row_err(val, full["W"][0][a:b]) < FP64_TOL
+
+
+def test_errors(pkg, gpu):
+    X, _ = grid(pkg, 16)
+    with pytest.raises(pkg.RbffdError) as e:
+        pkg.generate_operator(X, X, 3, len(X) + 1, 2)
+    assert e.value.code == 1
+    Xd = X.copy()
+    Xd[5] = Xd[6]  # duplicate node -> two identical rows in Phi -> singular (inv throws in Julia)
+    with pytest.raises(pkg.RbffdError) as e:
+        pkg.generate_operator(Xd, Xd, 3, 15, 2)
+    assert e.value.code == 3
+    Xn = X.copy()
+    Xn[3, 0] = np.nan
+    with pytest.raises(pkg.RbffdError) as e:
+        pkg.generate_operator(Xn, Xn, 3, 15, 2)
+    assert e.value.code == 1
+    # the handle stays usable after errors
+    E = pkg.generate_operator(X, X, 3, 15, 2, ops=("E",))[0]
+    assert np.allclose(E.toarray(), np.eye(len(X)), atol=1e-10)
