@@ -54,6 +54,24 @@ def dist_env():
     return ws, rank, local
 
 
+def shard_rows(rank, world, rows_per_rank):
+    """Evaluation rows of one rank (weak scaling: every rank owns rows_per_rank rows)."""
+    return rank * rows_per_rank, (rank + 1) * rows_per_rank
+
+
+def max_over_ranks(value, dist=None):
+    """Max of a per-rank float over all ranks (the job is as slow as its slowest rank)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+
+    backend = dist.get_backend()
+    dev = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def node_set(nx, ws):
     """Global node set: nx columns x (nx * ws) rows; rank r owns rows [r*nx^2, (r+1)*nx^2)."""
     import __graft_entry__
@@ -213,7 +231,7 @@ def run_ours(args):
     X_host, hgrid = node_set(args.nx, ws)
     N = len(X_host)
     rows_per = args.nx * args.nx
-    rb, re = rank * rows_per, (rank + 1) * rows_per
+    rb, re = shard_rows(rank, ws, rows_per)
     fp64_peak, fp32_peak = ctypes.c_double(), ctypes.c_double()
     L.rbffd_measure_fma_peaks(local, ctypes.byref(fp64_peak), ctypes.byref(fp32_peak))
 
@@ -285,11 +303,7 @@ def run_ours(args):
         dist.barrier()
     wall = time.perf_counter() - t_wall
     clocks = clk.stop()
-    ms_step = float(np.mean([t for t, _ in timed]))
-    if dist:
-        tt = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_step = float(tt.item())
+    ms_step = max_over_ranks(float(np.mean([t for t, _ in timed])), dist)
     total_rows = rows_per * ws
     value = total_rows / (ms_step * 1e-3)
 

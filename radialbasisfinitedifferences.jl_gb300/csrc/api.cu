@@ -68,7 +68,7 @@ struct Arena {
     {
         void *q = nullptr;
         size_t bytes = count * sizeof(T);
-        if (bytes == 0) bytes = 16;
+        if (bytes < 16) bytes = 16;
         cudaError_t e = cudaMallocAsync(&q, bytes, st);
         if (e != cudaSuccess) return e;
         ptrs.push_back(q);
@@ -423,6 +423,13 @@ RBFFD_EXPORT int rbffd_create(const rbffd_options *opt, rbffd_handle **out)
         return RBFFD_ECUDA;
     }
     h->num_sms = prop.multiProcessorCount;
+    // Keep freed stream-ordered memory in the device pool instead of returning it to the
+    // driver at every synchronisation: operator sets of ~1 GB are built and dropped per call.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         g_create_error = std::string("cuda: ") + cudaGetErrorString(e);
         delete h;
@@ -660,6 +667,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     a.nnz = nnz;
     a.max_s = max_s;
     a.max_n = max_n;
+    a.max_m = npoly_h(max_deg);
     a.first_bad = &dflags->first_bad;
     a.max_refine = h->opt.max_refine;
     a.refine_tol = h->opt.refine_tol;
@@ -670,8 +678,13 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         a.fallback_list = fb_list;
         a.fallback_count = &dflags->fallback_count;
         a.hist = dflags->hist;
-        int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(max_s, max_n, nops));
-        CK(launch_solve_mixed(a, table, wpb, h->num_sms, st));
+        cudaError_t e = launch_solve_mixed_reg(a, table, a.max_m, 4, h->num_sms, st);
+        if (e == cudaErrorNotSupported) {
+            cudaGetLastError();
+            int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(max_s, max_n, nops));
+            e = launch_solve_mixed(a, table, wpb, h->num_sms, st);
+        }
+        CK(e);
     } else {
         int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
         CK(launch_solve_fp64(a, table, wpb, h->num_sms, st));
@@ -864,9 +877,8 @@ RBFFD_EXPORT int rbffd_spmv(rbffd_handle *h, rbffd_opset *s, int op, const doubl
 {
     if (!h) return RBFFD_EINVAL;
     if (!s || op < 0 || op >= s->nops || !x || !y) return fail(h, RBFFD_EINVAL, "bad spmv arguments");
-    double avg = s->rows > 0 ? (double)s->nnz / s->rows : 0;
-    int group = avg >= 24 ? 32 : (avg >= 12 ? 16 : 8);
-    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, group, h->num_sms,
+    int kuni = s->uniform ? s->n : 0;  // uniform-stencil kernels need row r at r * n
+    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, kuni, h->num_sms,
                        h->stream));
     return RBFFD_OK;
 }

@@ -336,7 +336,10 @@ cudaError_t launch_grid_scatter(const double2 *X, const int32_t *cls, int64_t N,
 // ---------------------------------------------------------------------------
 namespace {
 
-__device__ __forceinline__ bool key_less(double da, int ia, double db, int ib)
+// Candidate keys: the IEEE bit pattern of a non-negative squared distance orders exactly
+// like the value, so (d2, id) is compared with integer instructions only (FP64 compares
+// run on the 1/64-rate FP64 pipe of GB300).
+__device__ __forceinline__ bool key_less(unsigned long long da, int ia, unsigned long long db, int ib)
 {
     return da < db || (da == db && ia < ib);
 }
@@ -348,11 +351,13 @@ __device__ __forceinline__ bool class_allowed(int cq, int cc)
     return cc >= 0 || cc == -b;
 }
 
+constexpr unsigned long long KEY_INF = 0x7ff0000000000000ull;  // bits of +inf
+
 template <int KS>
 struct TopK {
-    double d[KS];
+    unsigned long long d[KS];
     int id[KS];
-    double kd;  // current k-th key (warp uniform)
+    unsigned long long kd;  // current k-th key (warp uniform)
     int ki;
     int k;
 
@@ -360,18 +365,18 @@ struct TopK {
     {
 #pragma unroll
         for (int s = 0; s < KS; s++) {
-            d[s] = CUDART_INF;
+            d[s] = KEY_INF;
             id[s] = INT_MAX;
         }
-        kd = CUDART_INF;
+        kd = KEY_INF;
         ki = INT_MAX;
         k = kk;
     }
 
-    __device__ __forceinline__ void refresh_kth(int lane)
+    __device__ __forceinline__ void refresh_kth()
     {
         int t = k - 1, ss = t >> 5, sl = t & 31;
-        double v = d[0];
+        unsigned long long v = d[0];
         int vi = id[0];
 #pragma unroll
         for (int s = 1; s < KS; s++)
@@ -381,20 +386,19 @@ struct TopK {
             }
         kd = __shfl_sync(RBFFD_FULL, v, sl);
         ki = __shfl_sync(RBFFD_FULL, vi, sl);
-        (void)lane;
     }
 
-    __device__ __forceinline__ void insert(double cd, int ci, int lane)
+    __device__ __forceinline__ void insert(unsigned long long cd, int ci, int lane)
     {
         int pos = 0;
 #pragma unroll
         for (int s = 0; s < KS; s++) pos += __popc(__ballot_sync(RBFFD_FULL, key_less(d[s], id[s], cd, ci)));
 #pragma unroll
         for (int s = KS - 1; s >= 0; s--) {
-            double ud = __shfl_up_sync(RBFFD_FULL, d[s], 1);
+            unsigned long long ud = __shfl_up_sync(RBFFD_FULL, d[s], 1);
             int ui = __shfl_up_sync(RBFFD_FULL, id[s], 1);
             if (s > 0) {
-                double wd = __shfl_sync(RBFFD_FULL, d[s - 1], 31);
+                unsigned long long wd = __shfl_sync(RBFFD_FULL, d[s - 1], 31);
                 int wi = __shfl_sync(RBFFD_FULL, id[s - 1], 31);
                 if (lane == 0) {
                     ud = wd;
@@ -410,15 +414,14 @@ struct TopK {
                 id[s] = ci;
             }
         }
-        refresh_kth(lane);
+        refresh_kth();
     }
 };
 
 // Sweep the candidate segments [sa, sa+sl) held by lanes 0..nseg-1.
 template <int KS>
-__device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, int nseg,
-                                               int64_t sa, int sl, double qx, double qy, int cq,
-                                               int lane)
+__device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, int nseg, int64_t sa, int sl,
+                                               double qx, double qy, int cq, int lane)
 {
     // exclusive offsets of the segments
     int inc = sl;
@@ -439,7 +442,7 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
         }
         int64_t a = __shfl_sync(RBFFD_FULL, sa, seg);
         int os = __shfl_sync(RBFFD_FULL, off, seg);
-        double cd = CUDART_INF;
+        unsigned long long cd = KEY_INF;
         int ci = INT_MAX;
         if (pos < total) {
             int64_t t = a + (pos - os);
@@ -447,7 +450,7 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
             if (class_allowed(cq, cc)) {
                 double2 p = g.pts[t];
                 double dx = __dsub_rn(qx, p.x), dy = __dsub_rn(qy, p.y);
-                cd = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+                cd = (unsigned long long)__double_as_longlong(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 ci = g.ids[t];
             }
         }
@@ -455,7 +458,7 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
         while (m) {
             int src = __ffs(m) - 1;
             m &= m - 1;
-            double sd = __shfl_sync(RBFFD_FULL, cd, src);
+            unsigned long long sd = __shfl_sync(RBFFD_FULL, cd, src);
             int si = __shfl_sync(RBFFD_FULL, ci, src);
             if (key_less(sd, si, tk.kd, tk.ki)) tk.insert(sd, si, lane);
         }
@@ -542,17 +545,18 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
             if (cy - R > 0) bound = fmin(bound, qp.y - (g.y0 + (cy - R) * g.cs));
             if (cy + R < g.ny - 1) bound = fmin(bound, (g.y0 + (cy + R + 1) * g.cs) - qp.y);
             if (bound == CUDART_INF) done = true;
-            else if (bound > 0 && tk.kd < bound * bound * (1.0 - 1e-12)) done = true;
+            else if (bound > 0 && tk.kd < (unsigned long long)__double_as_longlong(bound * bound * (1.0 - 1e-12)))
+                done = true;
         }
         int64_t ob = out_ptr ? out_ptr[node] : node * (int64_t)k;
-        bool short_list = !(tk.kd < CUDART_INF);
+        bool short_list = !(tk.kd < KEY_INF);
         if (short_list && lane == 0) atomicOr(err_flag, 1);
 #pragma unroll
         for (int s = 0; s < KS; s++) {
             int t = s * 32 + lane;
             if (t < k) {
                 out_idx[ob + t] = short_list ? -1 : tk.id[s];
-                if (out_d2) out_d2[ob + t] = tk.d[s];
+                if (out_d2) out_d2[ob + t] = __longlong_as_double((long long)tk.d[s]);
             }
         }
     }

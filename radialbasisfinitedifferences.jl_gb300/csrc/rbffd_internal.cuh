@@ -120,7 +120,7 @@ struct SolveArgs {
     int32_t *col;              // nnz
     double *val;               // nops * nnz (op-major)
     int64_t nnz;
-    int max_s, max_n;          // largest s / n over the systems (smem sizing)
+    int max_s, max_n, max_m;   // largest s / n / m over the systems (smem sizing)
     int64_t *first_bad;        // atomicMin of failing node (init INT64_MAX)
     int32_t *fallback_list;    // mixed: systems needing FP64 (nullable for plain)
     int *fallback_count;
@@ -134,6 +134,11 @@ cudaError_t launch_solve_fp64(const SolveArgs &a, const OpTable &ops, int warps_
                               int num_sms, cudaStream_t st);
 cudaError_t launch_solve_mixed(const SolveArgs &a, const OpTable &ops, int warps_per_block,
                                int num_sms, cudaStream_t st);
+// Register-resident FP32 factorisation (max_s <= 64, nops <= 6); cudaErrorNotSupported
+// for other shapes.
+cudaError_t launch_solve_mixed_reg(const SolveArgs &a, const OpTable &ops, int max_m, int warps_per_block,
+                                   int num_sms, cudaStream_t st);
+size_t solve_mixed_reg_smem_per_warp(int S, int max_n, int max_m, int nops);
 // FP64 re-solve of the systems the mixed kernel queued in a.fallback_list.
 cudaError_t launch_solve_fp64_subset(const SolveArgs &a, const OpTable &ops, int warps_per_block,
                                      int num_sms, cudaStream_t st, int64_t count);

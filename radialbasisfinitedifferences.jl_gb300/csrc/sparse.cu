@@ -7,26 +7,60 @@
 
 namespace {
 
-// One group of G lanes per row; the row's entries are read by consecutive lanes (coalesced),
-// reduced by shuffles inside the group (fixed order: deterministic results).
-template <int G>
-__global__ void __launch_bounds__(256) spmv_f64_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
-                                                       const int32_t *__restrict__ col,
-                                                       const double *__restrict__ val,
-                                                       const double *__restrict__ x,
-                                                       double *__restrict__ y)
+// SpMV, one thread per row.  GB300 runs FP64 at 1/64 of the FP32 rate and an FP64 warp
+// instruction costs the same whatever its active mask, so a cross-lane reduction of partial
+// sums (5 FP64 adds per row) would cost more than the row's own FMAs; here every FP64
+// instruction is one lane's FMA of its own row.  All of a row's weight and index loads are
+// independent and issued before the x gathers (streaming hints keep x in L2).
+__global__ void __launch_bounds__(256) spmv_f64_rows(int64_t rows, const int64_t *__restrict__ row_ptr,
+                                                     const int32_t *__restrict__ col,
+                                                     const double *__restrict__ val,
+                                                     const double *__restrict__ x, double *__restrict__ y)
 {
-    int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t group = tid / G;
-    int gl = threadIdx.x & (G - 1);
-    int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
-    for (int64_t r = group; r < rows; r += ngroups) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
         int64_t a = row_ptr[r], b = row_ptr[r + 1];
         double acc = 0.0;
-        for (int64_t t = a + gl; t < b; t += G) acc = fma(__ldcs(val + t), __ldg(x + __ldcs(col + t)), acc);
+        int64_t t = a;
+        for (; t + 4 <= b; t += 4) {
+            double w0 = __ldcs(val + t), w1 = __ldcs(val + t + 1), w2 = __ldcs(val + t + 2), w3 = __ldcs(val + t + 3);
+            int c0 = __ldcs(col + t), c1 = __ldcs(col + t + 1), c2 = __ldcs(col + t + 2), c3 = __ldcs(col + t + 3);
+            acc = fma(w0, __ldg(x + c0), acc);
+            acc = fma(w1, __ldg(x + c1), acc);
+            acc = fma(w2, __ldg(x + c2), acc);
+            acc = fma(w3, __ldg(x + c3), acc);
+        }
+        for (; t < b; t++) acc = fma(__ldcs(val + t), __ldg(x + __ldcs(col + t)), acc);
+        __stcs(y + r, acc);
+    }
+}
+
+// Uniform stencil size K (even): row r occupies [r*K, r*K + K); 16-byte weight loads and
+// 8-byte index loads, fully unrolled.
+template <int K>
+__global__ void __launch_bounds__(256) spmv_f64_uniform(int64_t rows, const int32_t *__restrict__ col,
+                                                        const double *__restrict__ val,
+                                                        const double *__restrict__ x, double *__restrict__ y)
+{
+    static_assert(K % 2 == 0, "even K");
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const double2 *v2 = reinterpret_cast<const double2 *>(val + r * K);
+        const int2 *c2 = reinterpret_cast<const int2 *>(col + r * K);
+        double2 w[K / 2];
+        int2 c[K / 2];
 #pragma unroll
-        for (int o = G / 2; o; o >>= 1) acc += __shfl_xor_sync(RBFFD_FULL, acc, o, G);
-        if (gl == 0) __stcs(y + r, acc);
+        for (int i = 0; i < K / 2; i++) {
+            w[i] = __ldcs(v2 + i);
+            c[i] = __ldcs(c2 + i);
+        }
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < K / 2; i++) {
+            acc = fma(w[i].x, __ldg(x + c[i].x), acc);
+            acc = fma(w[i].y, __ldg(x + c[i].y), acc);
+        }
+        __stcs(y + r, acc);
     }
 }
 
@@ -181,13 +215,13 @@ cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t 
 {
     if (rows <= 0) return cudaSuccess;
     int threads = 256;
-    int64_t want = (rows * group + threads - 1) / threads;
-    int64_t cap = (int64_t)num_sms * 8 * 4;
-    int blocks = (int)(want < cap ? want : cap);
+    int blocks = blocks_for(rows, threads, (int64_t)num_sms * 64);
+    // `group` carries the uniform stencil size (0 = general CSR)
     switch (group) {
-    case 8: spmv_f64_kernel<8><<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
-    case 16: spmv_f64_kernel<16><<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
-    default: spmv_f64_kernel<32><<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
+    case 20: spmv_f64_uniform<20><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
+    case 30: spmv_f64_uniform<30><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
+    case 42: spmv_f64_uniform<42><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
+    default: spmv_f64_rows<<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
     }
     return cudaGetLastError();
 }

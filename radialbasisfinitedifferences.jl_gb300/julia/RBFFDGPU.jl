@@ -1,0 +1,220 @@
+"""
+    RBFFDGPU
+
+Julia host side of librbffd (include/rbffd.h): the methods of
+RadialBasisFiniteDifferences.jl's operator API -- `generate_operator`,
+`hyperviscosity_operator`, `calculateneighbors` -- with the same arguments and return
+values (`SparseMatrixCSC{Float64,Int64}`), computed on a GB300 through `ccall`.
+
+The library writes the CSC arrays (1-based `colptr`/`rowval`, `nzval`) straight into
+Julia-owned vectors, so no copy is made on the Julia side.  A singular local system
+raises `LinearAlgebra.SingularException` as `inv` does in the reference
+(src/interpolationmatrix.jl:8); every other failure raises `ErrorException`.
+"""
+module RBFFDGPU
+
+using LinearAlgebra
+using SparseArrays
+using StaticArrays
+
+const LIB = get(ENV, "RBFFD_LIB", joinpath(@__DIR__, "..", "_lib", "librbffd.so"))
+
+const OP = (E = 0, Dx = 1, Dy = 2, Dxx = 3, Dyy = 4, Dxy = 5, Lap = 6, Dxk = 7, Dyk = 8, HV = 9)
+const PREC = (fp64 = Cint(0), mixed = Cint(1))
+mask(ops) = reduce(|, (UInt32(1) << getfield(OP, o) for o in ops))
+const GENERATE = (:E, :Dx, :Dy, :Dxx, :Dyy, :Dxy)
+
+struct Options
+    device::Cint
+    warps_per_block::Cint
+    max_refine::Cint
+    refine_tol::Cdouble
+end
+
+struct Stats
+    ms_upload::Cdouble
+    ms_grid::Cdouble
+    ms_knn::Cdouble
+    ms_solve::Cdouble
+    ms_fallback::Cdouble
+    ms_csr::Cdouble
+    ms_total::Cdouble
+    n_systems::Int64
+    n_rows::Int64
+    n_fallback::Int64
+    first_bad_node::Int64
+    refine_hist::NTuple{8,Int64}
+    nnz::Int64
+    kernel_launches::Int64
+end
+Stats() = Stats(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, -1, ntuple(_ -> 0, 8), 0, 0)
+
+struct CSC
+    colptr::Ptr{Int64}
+    rowval::Ptr{Int64}
+    nzval::Ptr{Float64}
+end
+
+mutable struct Handle
+    ptr::Ptr{Cvoid}
+end
+
+function Handle(; device::Integer = 0, warps_per_block::Integer = 0)
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    opt = Ref(Options(device, warps_per_block, 0, 0.0))
+    rc = ccall((:rbffd_create, LIB), Cint, (Ref{Options}, Ref{Ptr{Cvoid}}), opt, ref)
+    rc == 0 || error("rbffd_create: ", unsafe_string(ccall((:rbffd_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+    h = Handle(ref[])
+    finalizer(h) do x
+        x.ptr == C_NULL || ccall((:rbffd_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr)
+        x.ptr = C_NULL
+    end
+    return h
+end
+
+const _handle = Ref{Union{Nothing,Handle}}(nothing)
+handle() = something(_handle[], (_handle[] = Handle()))
+
+function check(h::Handle, rc, stats::Ref{Stats})
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:rbffd_last_error, LIB), Cstring, (Ptr{Cvoid},), h.ptr))
+    rc == 3 && throw(SingularException(Int(stats[].first_bad_node) + 1))
+    error("librbffd error $rc: $msg")
+end
+
+points(X) = convert(Vector{SVector{2,Float64}}, X)
+
+"Node classes from the index ranges of calculateneighbors: 0 interior, +b boundary b, -b ghost of b."
+function node_class(N, X_idx_in, X_idx_bc, X_idx_bc_g)
+    c = fill(typemin(Int32), N)
+    c[X_idx_in] .= 0
+    for (b, r) in enumerate(X_idx_bc)
+        c[r] .= b
+    end
+    for (b, r) in enumerate(X_idx_bc_g)
+        c[r] .= -b
+    end
+    any(==(typemin(Int32)), c) && throw(ArgumentError("every node must be in X_idx_in, X_idx_bc or X_idx_bc_g"))
+    return c
+end
+
+function alloc_csc(M, N, n, nops)
+    mats = [(Vector{Int64}(undef, N + 1), Vector{Int64}(undef, M * n), Vector{Float64}(undef, M * n)) for _ in 1:nops]
+    structs = [CSC(pointer(a), pointer(b), pointer(c)) for (a, b, c) in mats]
+    return mats, structs
+end
+
+tocsc(M, N, m) = SparseMatrixCSC(M, N, m[1], m[2], m[3])
+
+function _generate(X, Y, p, n, polydeg, cls, ops; precision = :fp64, h = handle())
+    Xv = points(X)
+    Yv = Y === X ? Xv : points(Y)
+    N, M = length(Xv), length(Yv)
+    order = sort(collect(ops); by = o -> getfield(OP, o))
+    mats, structs = alloc_csc(M, N, n, length(order))
+    stats = Ref(Stats())
+    GC.@preserve Xv Yv cls mats begin
+        rc = ccall((:rbffd_generate_operator, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Cint, Cint, Cint, Ptr{Int32}, UInt32, Cint,
+             Ptr{CSC}, Ref{Stats}),
+            h.ptr, pointer(reinterpret(Float64, Xv)), N, pointer(reinterpret(Float64, Yv)), M, p, n, polydeg,
+            cls === nothing ? C_NULL : pointer(cls), mask(order), getfield(PREC, precision), structs, stats)
+    end
+    check(h, rc, stats)
+    byop = Dict(o => tocsc(M, N, m) for (o, m) in zip(order, mats))
+    return Tuple(byop[o] for o in ops)
+end
+
+"generate_operator(X, Y, p, n, polydeg) -- src/generate_operator.jl:29-190"
+generate_operator(X, Y, p, n, polydeg; kw...) = _generate(X, Y, p, n, polydeg, nothing, GENERATE; kw...)
+
+"Boundary-aware overload -- src/generate_operator.jl:192-352"
+function generate_operator(X, Y, p, n, polydeg, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc, Y_idx_bc_g; kw...)
+    cls = node_class(length(X), X_idx_in, X_idx_bc, X_idx_bc_g)
+    return _generate(X, Y, p, n, polydeg, cls, GENERATE; kw...)
+end
+
+"Collocated, unscaled overload -- src/generate_operator.jl:354-491 (reproduced as computed there)"
+function generate_operator(X, p::Integer, n::Integer, polydeg::Integer; h = handle())
+    Xv = points(X)
+    N = length(Xv)
+    mats, structs = alloc_csc(N, N, n, 6)
+    stats = Ref(Stats())
+    GC.@preserve Xv mats begin
+        rc = ccall((:rbffd_generate_operator_unscaled, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint, Cint, Cint, UInt32, Cint, Ptr{CSC}, Ref{Stats}),
+            h.ptr, pointer(reinterpret(Float64, Xv)), N, p, n, polydeg, mask(GENERATE), 0, structs, stats)
+    end
+    check(h, rc, stats)
+    return Tuple(tocsc(N, N, m) for m in mats)
+end
+
+function _hyper(k_deriv, X, Y, p, n, polydeg, cls; precision = :fp64, h = handle())
+    Xv = points(X)
+    Yv = Y === X ? Xv : points(Y)
+    N, M = length(Xv), length(Yv)
+    mats, structs = alloc_csc(M, N, n, 2)
+    stats = Ref(Stats())
+    GC.@preserve Xv Yv cls mats begin
+        rc = ccall((:rbffd_hyperviscosity_operator, LIB), Cint,
+            (Ptr{Cvoid}, Cint, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Cint, Cint, Cint, Ptr{Int32}, Cint,
+             Ptr{CSC}, Ref{Stats}),
+            h.ptr, k_deriv, pointer(reinterpret(Float64, Xv)), N, pointer(reinterpret(Float64, Yv)), M, p, n,
+            polydeg, cls === nothing ? C_NULL : pointer(cls), getfield(PREC, precision), structs, stats)
+    end
+    check(h, rc, stats)
+    return tocsc(M, N, mats[1]), tocsc(M, N, mats[2])
+end
+
+"hyperviscosity_operator(k_deriv, X, Y, p, n, polydeg) -- src/hyperviscosity_operator.jl:26-175"
+hyperviscosity_operator(k_deriv, X, Y, p, n, polydeg; kw...) = _hyper(k_deriv, X, Y, p, n, polydeg, nothing; kw...)
+
+"Boundary-aware overload -- src/hyperviscosity_operator.jl:177-312"
+function hyperviscosity_operator(k_deriv, X, Y, p, n, polydeg, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc,
+                                 Y_idx_bc_g; kw...)
+    cls = node_class(length(X), X_idx_in, X_idx_bc, X_idx_bc_g)
+    return _hyper(k_deriv, X, Y, p, n, polydeg, cls; kw...)
+end
+
+"Collocated, unscaled overload -- src/hyperviscosity_operator.jl:314-440"
+function hyperviscosity_operator(k_deriv::Integer, X, p::Integer, n::Integer, polydeg::Integer; h = handle())
+    Xv = points(X)
+    N = length(Xv)
+    mats, structs = alloc_csc(N, N, n, 2)
+    stats = Ref(Stats())
+    GC.@preserve Xv mats begin
+        rc = ccall((:rbffd_generate_operator_unscaled, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint, Cint, Cint, UInt32, Cint, Ptr{CSC}, Ref{Stats}),
+            h.ptr, pointer(reinterpret(Float64, Xv)), N, p, n, polydeg, mask((:Dxk, :Dyk)), k_deriv, structs, stats)
+    end
+    check(h, rc, stats)
+    return tocsc(N, N, mats[1]), tocsc(N, N, mats[2])
+end
+
+"calculateneighbors(X, Y, n, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc, Y_idx_bc_g) -- src/calculateneighbors.jl:1-97"
+function calculateneighbors(X, Y, n, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc, Y_idx_bc_g; h = handle())
+    Xv, Yv = points(X), points(Y)
+    N, M = length(Xv), length(Yv)
+    cls = node_class(N, X_idx_in, X_idx_bc, X_idx_bc_g)
+    ix = Matrix{Int64}(undef, n, N)   # column i = stencil of node i (row-major N x n on the C side)
+    dx = Matrix{Float64}(undef, n, N)
+    iy = Vector{Int64}(undef, M)
+    dy = Vector{Float64}(undef, M)
+    GC.@preserve Xv Yv cls ix dx iy dy begin
+        rc = ccall((:rbffd_calculateneighbors, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Cint, Ptr{Int32}, Ptr{Int64}, Ptr{Float64},
+             Ptr{Int64}, Ptr{Float64}),
+            h.ptr, pointer(reinterpret(Float64, Xv)), N, pointer(reinterpret(Float64, Yv)), M, n, pointer(cls),
+            pointer(ix), pointer(dx), pointer(iy), pointer(dy))
+    end
+    check(h, rc, Ref(Stats()))
+    idxs_x = [SVector{n}(view(ix, :, i)) for i in 1:N]
+    dists_x = [SVector{n}(view(dx, :, i)) for i in 1:N]
+    idxs_y_x = [SVector{1}(iy[i]) for i in 1:M]
+    dists_y_x = [SVector{1}(dy[i]) for i in 1:M]
+    return idxs_x, idxs_y_x, dists_x, dists_y_x
+end
+
+export generate_operator, hyperviscosity_operator, calculateneighbors
+
+end # module
