@@ -206,6 +206,29 @@ int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, 
                int dtype);
 
 /* ---------------------------------------------------------------------------------
+ * Allocation-free kNN (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory: hosts whose device memory belongs to
+ * another allocator that must not be bypassed (a CUDA.jl or PyTorch caching pool),
+ * programs with a device-memory budget fixed at start-up, and code that must not
+ * synchronise the device as cudaMalloc/cudaFree may.  The stencils of all N nodes
+ * (k nearest, self first, ties by lower id -- the same sets as rbffd_calculateneighbors)
+ * are written to caller-owned device buffers: idx_dev (N x k, 0-based int32) and d2_dev
+ * (N x k squared distances, nullable).  X_dev: N device points (AoS, 16-byte aligned).
+ * stream: a cudaStream_t (NULL = default stream); the call synchronises it.
+ *
+ * Scratch lives in one static device array of RBFFD_NOALLOC_SCRATCH_BYTES per GPU, held
+ * until the process exits; N above RBFFD_NOALLOC_MAX_NODES is rejected with RBFFD_EINVAL
+ * (message in rbffd_last_error(NULL)).  The first call on each device looks the array's
+ * address up (make it before any stream capture).  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.
+ * ------------------------------------------------------------------------------ */
+#define RBFFD_NOALLOC_MAX_NODES 65536
+#define RBFFD_NOALLOC_SCRATCH_BYTES (5u << 20)
+int rbffd_knn_noalloc(const double *X_dev, int64_t N, int k, int32_t *idx_dev, double *d2_dev,
+                      void *stream);
+
+/* ---------------------------------------------------------------------------------
  * Diagnostics.
  * ------------------------------------------------------------------------------ */
 

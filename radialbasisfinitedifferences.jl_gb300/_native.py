@@ -36,6 +36,7 @@ EXPORTED = [
     "rbffd_opset_export_stencils",
     "rbffd_spmv",
     "rbffd_spmm",
+    "rbffd_knn_noalloc",
     "rbffd_measure_fma_peaks",
 ]
 
@@ -149,6 +150,7 @@ def load(build_if_missing=False):
         "rbffd_opset_export_stencils": ([P, P, P, P], i32),
         "rbffd_spmv": ([P, P, i32, P, P], i32),
         "rbffd_spmm": ([P, P, i32, P, P, i32, i32], i32),
+        "rbffd_knn_noalloc": ([P, i64, i32, P, P, P], i32),
         "rbffd_measure_fma_peaks": ([i32, P, P], i32),
     }
     for name, (args, res) in sig.items():

@@ -337,6 +337,8 @@ int autotune_wpb(rbffd_handle *h, size_t per_warp)
 
 }  // namespace
 
+void set_handleless_error(const std::string &msg) { g_create_error = msg; }
+
 bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, std::string *err)
 {
     memset(t, 0, sizeof(*t));

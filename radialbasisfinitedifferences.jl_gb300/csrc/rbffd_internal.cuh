@@ -47,6 +47,9 @@ struct OpTable {
     OpDesc op[RBFFD_MAX_OPS];
 };
 
+// Text returned by rbffd_last_error(NULL) on this thread (errors of calls without a handle).
+void set_handleless_error(const std::string &msg);
+
 // Build the descriptor table for the ops in `ops` (RBFFD_OP_* codes).
 bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, std::string *err);
 
