@@ -206,6 +206,26 @@ int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, 
                int dtype);
 
 /* ---------------------------------------------------------------------------------
+ * Time stepping: explicit RK4 for du/dt = L u on nfields fields, the semi-discrete system
+ * the reference integrates in examples/adv_diff_test.jl:144-199 (cons_sys, SSPRK43).
+ * ------------------------------------------------------------------------------ */
+
+/* L = sum over the sets' operators of coef[i] * A_i, in set order then operator order
+   (sets: collocated, full, built from one node set with one stencil size, so they share a
+   sparsity pattern; e.g. {Dx, Dy, Lap} with r^3 and {HV} with r^5).  fixed_rows (host,
+   nullable, rows bytes): rows held at their initial values (du = 0), the Dirichlet
+   overwrite of examples/adv_diff_test.jl:166-167.  dtype 0: FP64 weights and fields,
+   1: FP32.  Fields are row-major [rows][nfields] device arrays. */
+int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int nsets, const double *coef,
+                     const uint8_t *fixed_rows, int nfields, int dtype, rbffd_rk4 **out);
+/* Advance u (device, in place) by nsteps steps of size dt.  Pairs of steps run as one
+   captured CUDA graph (4 fused stage kernels per step), re-captured when u or dt change. */
+int rbffd_rk4_run(rbffd_handle *h, rbffd_rk4 *rk, void *u, double dt, int64_t nsteps);
+/* y = L x for the stepper's fields (x, y device [rows][nfields]). */
+int rbffd_rk4_apply(rbffd_handle *h, rbffd_rk4 *rk, const void *x, void *y);
+void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk);
+
+/* ---------------------------------------------------------------------------------
  * Allocation-free kNN (no counterpart in the reference).
  *
  * For callers that cannot allocate device memory: hosts whose device memory belongs to

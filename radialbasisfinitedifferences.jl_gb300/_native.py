@@ -36,6 +36,10 @@ EXPORTED = [
     "rbffd_opset_export_stencils",
     "rbffd_spmv",
     "rbffd_spmm",
+    "rbffd_rk4_create",
+    "rbffd_rk4_run",
+    "rbffd_rk4_apply",
+    "rbffd_rk4_destroy",
     "rbffd_knn_noalloc",
     "rbffd_measure_fma_peaks",
 ]
@@ -150,6 +154,10 @@ def load(build_if_missing=False):
         "rbffd_opset_export_stencils": ([P, P, P, P], i32),
         "rbffd_spmv": ([P, P, i32, P, P], i32),
         "rbffd_spmm": ([P, P, i32, P, P, i32, i32], i32),
+        "rbffd_rk4_create": ([P, P, i32, P, P, i32, i32, P], i32),
+        "rbffd_rk4_run": ([P, P, P, ctypes.c_double, i64], i32),
+        "rbffd_rk4_apply": ([P, P, P, P], i32),
+        "rbffd_rk4_destroy": ([P, P], None),
         "rbffd_knn_noalloc": ([P, i64, i32, P, P, P], i32),
         "rbffd_measure_fma_peaks": ([i32, P, P], i32),
     }

@@ -907,6 +907,173 @@ RBFFD_EXPORT int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void 
 }
 
 // ---------------------------------------------------------------------------
+// RK4 time stepping on device-resident operators.
+// ---------------------------------------------------------------------------
+struct rbffd_rk4 {
+    int64_t rows = 0, nnz = 0;
+    int F = 0, dtype = 0;
+    int64_t *row_ptr = nullptr;
+    int32_t *col = nullptr;
+    double *val64 = nullptr;
+    float *val32 = nullptr;
+    uint8_t *fixed = nullptr;
+    void *unext = nullptr, *wA = nullptr, *wB = nullptr, *acc = nullptr;
+    cudaGraphExec_t graph2 = nullptr;  // two steps u -> unext -> u
+    const void *graph_u = nullptr;
+    double graph_dt = 0.0;
+    std::vector<void *> owned;
+};
+
+namespace {
+// Enqueue one RK4 step u -> out on stream st.
+cudaError_t rk4_enqueue_step(rbffd_handle *h, rbffd_rk4 *rk, const void *u, void *out, double dt, cudaStream_t st)
+{
+    const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
+    cudaError_t e;
+    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, u, u, rk->acc, rk->wA, rk->fixed, rk->F, 0.5 * dt, 0,
+                         rk->dtype, h->num_sms, st);
+    if (e != cudaSuccess) return e;
+    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, rk->wB, rk->fixed, rk->F, 0.5 * dt,
+                         1, rk->dtype, h->num_sms, st);
+    if (e != cudaSuccess) return e;
+    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wB, u, rk->acc, rk->wA, rk->fixed, rk->F, dt, 1,
+                         rk->dtype, h->num_sms, st);
+    if (e != cudaSuccess) return e;
+    return launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, out, rk->fixed, rk->F, dt / 6.0,
+                            2, rk->dtype, h->num_sms, st);
+}
+}  // namespace
+
+RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int nsets, const double *coef,
+                                  const uint8_t *fixed_rows, int nfields, int dtype, rbffd_rk4 **out)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!sets || nsets <= 0 || !coef || !out || nfields <= 0 || (dtype != 0 && dtype != 1))
+        return fail(h, RBFFD_EINVAL, "bad rk4 arguments");
+    *out = nullptr;
+    cudaSetDevice(h->device);
+    const rbffd_opset *s0 = sets[0];
+    for (int i = 0; i < nsets; i++) {
+        const rbffd_opset *s = sets[i];
+        if (!s || !s->collocated || s->row_begin != 0 || s->rows != s->N || s->N != s0->N || s->nnz != s0->nnz)
+            return fail(h, RBFFD_EINVAL, "rk4 needs collocated full operator sets of one node set");
+    }
+    cudaStream_t st = h->stream;
+    Arena keep(st), tmp(st);
+    int nq = 0;
+    for (int i = 0; i < nsets; i++) nq += sets[i]->nops;
+    std::vector<const double *> hv;
+    for (int i = 0; i < nsets; i++)
+        for (int q = 0; q < sets[i]->nops; q++) hv.push_back(sets[i]->val + (size_t)q * sets[i]->nnz);
+    // every set must share the first set's stencils
+    unsigned long long *diff;
+    CK(tmp.zeros(&diff, 1));
+    for (int i = 1; i < nsets; i++) CK(launch_count_diff(s0->nnz, s0->col, sets[i]->col, diff, st));
+    unsigned long long hdiff = 0;
+    CK(cudaMemcpyAsync(&hdiff, diff, sizeof(hdiff), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hdiff) return fail(h, RBFFD_EINVAL, "operator sets do not share one stencil pattern");
+    rbffd_rk4 *rk = new rbffd_rk4();
+    rk->rows = s0->rows;
+    rk->nnz = s0->nnz;
+    rk->F = nfields;
+    rk->dtype = dtype;
+    auto bail = [&](int code) {
+        delete rk;
+        return code;
+    };
+    const double **dvals;
+    double *dcoef;
+    cudaError_t e = cudaSuccess;
+#define CKB(expr)                                                                                            \
+    do {                                                                                                     \
+        e = (expr);                                                                                          \
+        if (e != cudaSuccess) return bail(fail(h, RBFFD_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e))); \
+    } while (0)
+    CKB(tmp.get(&dvals, nq));
+    CKB(tmp.get(&dcoef, nq));
+    CKB(cudaMemcpyAsync(dvals, hv.data(), sizeof(double *) * nq, cudaMemcpyHostToDevice, st));
+    CKB(cudaMemcpyAsync(dcoef, coef, sizeof(double) * nq, cudaMemcpyHostToDevice, st));
+    CKB(keep.get(&rk->row_ptr, rk->rows + 1));
+    CKB(keep.get(&rk->col, rk->nnz));
+    CKB(keep.get(&rk->val64, rk->nnz));
+    CKB(keep.get(&rk->val32, rk->nnz));
+    CKB(cudaMemcpyAsync(rk->row_ptr, s0->row_ptr, sizeof(int64_t) * (rk->rows + 1), cudaMemcpyDeviceToDevice, st));
+    CKB(cudaMemcpyAsync(rk->col, s0->col, sizeof(int32_t) * rk->nnz, cudaMemcpyDeviceToDevice, st));
+    CKB(launch_combine_ops(rk->nnz, dvals, dcoef, nq, rk->val64, rk->val32, st));
+    if (fixed_rows) {
+        CKB(keep.get(&rk->fixed, rk->rows));
+        CKB(cudaMemcpyAsync(rk->fixed, fixed_rows, rk->rows, cudaMemcpyHostToDevice, st));
+    }
+    size_t fb = (size_t)rk->rows * nfields * (dtype == 0 ? 8 : 4);
+    char *bufs;
+    CKB(keep.get(&bufs, 4 * fb));
+    rk->unext = bufs;
+    rk->wA = bufs + fb;
+    rk->wB = bufs + 2 * fb;
+    rk->acc = bufs + 3 * fb;
+    CKB(cudaStreamSynchronize(st));
+#undef CKB
+    keep.release_to(rk->owned);
+    *out = rk;
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_rk4_apply(rbffd_handle *h, rbffd_rk4 *rk, const void *x, void *y)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!rk || !x || !y) return fail(h, RBFFD_EINVAL, "bad rk4_apply arguments");
+    const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
+    CK(launch_spmm(rk->rows, rk->row_ptr, rk->col, val, x, y, rk->F, rk->dtype, h->stream));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT int rbffd_rk4_run(rbffd_handle *h, rbffd_rk4 *rk, void *u, double dt, int64_t nsteps)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!rk || !u || nsteps < 0) return fail(h, RBFFD_EINVAL, "bad rk4_run arguments");
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    if (nsteps >= 2 && (!rk->graph2 || rk->graph_u != u || rk->graph_dt != dt)) {
+        if (rk->graph2) {
+            cudaGraphExecDestroy(rk->graph2);
+            rk->graph2 = nullptr;
+        }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e1 = rk4_enqueue_step(h, rk, u, rk->unext, dt, st);
+        cudaError_t e2 = e1 == cudaSuccess ? rk4_enqueue_step(h, rk, rk->unext, u, dt, st) : e1;
+        cudaError_t e3 = cudaStreamEndCapture(st, &g);
+        CK(e2);
+        CK(e3);
+        cudaError_t e4 = cudaGraphInstantiate(&rk->graph2, g, 0);
+        cudaGraphDestroy(g);
+        CK(e4);
+        rk->graph_u = u;
+        rk->graph_dt = dt;
+    }
+    for (int64_t i = 0; i + 2 <= nsteps; i += 2) CK(cudaGraphLaunch(rk->graph2, st));
+    if (nsteps % 2) {
+        CK(rk4_enqueue_step(h, rk, u, rk->unext, dt, st));
+        size_t fb = (size_t)rk->rows * rk->F * (rk->dtype == 0 ? 8 : 4);
+        CK(cudaMemcpyAsync(u, rk->unext, fb, cudaMemcpyDeviceToDevice, st));
+    }
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk)
+{
+    if (!rk) return;
+    if (rk->graph2) cudaGraphExecDestroy(rk->graph2);
+    if (h) {
+        cudaSetDevice(h->device);
+        for (void *p : rk->owned) cudaFreeAsync(p, h->stream);
+        cudaStreamSynchronize(h->stream);
+    }
+    delete rk;
+}
+
+// ---------------------------------------------------------------------------
 // Drop-in entry points.
 // ---------------------------------------------------------------------------
 static int export_all(rbffd_handle *h, rbffd_opset *s, rbffd_csc *out)

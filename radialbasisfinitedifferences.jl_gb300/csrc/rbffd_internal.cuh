@@ -155,6 +155,14 @@ cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t 
 cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col,
                         const void *val, const void *x, void *y, int nfields, int dtype,
                         cudaStream_t st);
+// RK4 stage (mode 0: first stage, 1: middle stages, 2: last stage), see sparse.cu.
+cudaError_t launch_rk4_stage(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
+                             const void *w, const void *u, void *acc, void *out, const uint8_t *fixed, int F,
+                             double c, int mode, int dtype, int num_sms, cudaStream_t st);
+cudaError_t launch_combine_ops(int64_t nnz, const double *const *vals, const double *coef, int nq,
+                               double *out64, float *out32, cudaStream_t st);
+cudaError_t launch_count_diff(int64_t n, const int32_t *a, const int32_t *b, unsigned long long *cnt,
+                              cudaStream_t st);
 cudaError_t launch_csc_count(int64_t nnz, const int32_t *col, int64_t *colcount,
                              cudaStream_t st);
 cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32_t *col,

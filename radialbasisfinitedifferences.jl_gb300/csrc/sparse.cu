@@ -64,6 +64,54 @@ __global__ void __launch_bounds__(256) spmv_f64_uniform(int64_t rows, const int3
     }
 }
 
+// Uniform stencil size K (even), staged: each warp owns tiles of 32 consecutive rows, whose
+// weights (32*K doubles) and column ids (32*K ints) are contiguous in HBM.  The warp copies
+// a tile into its shared-memory slot with fully coalesced 16-byte loads (4 L1 wavefronts per
+// instruction instead of 32 for per-thread row loads), then each lane accumulates its own
+// row from shared memory (row stride K*8 bytes = odd multiple of 16 for K = 2 mod 4:
+// conflict-free LDS.128) with x gathered through L1/L2.
+template <int K>
+__global__ void __launch_bounds__(256) spmv_f64_staged(int64_t rows, const int32_t *__restrict__ col,
+                                                       const double *__restrict__ val,
+                                                       const double *__restrict__ x, double *__restrict__ y)
+{
+    static_assert(K % 2 == 0, "even K");
+    constexpr int VB = 32 * K * 8, CB = 32 * K * 4;
+    extern __shared__ __align__(16) unsigned char sm_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned char *mine = sm_dyn + (size_t)w * (VB + CB);
+    double *sv = reinterpret_cast<double *>(mine);
+    int *sc = reinterpret_cast<int *>(mine + VB);
+    int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t ntile = (rows + 31) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (; tile < ntile; tile += nw) {
+        const int64_t r0 = tile * 32;
+        const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
+        const int nv2 = nr * K / 2;  // double2 chunks
+        const double2 *gv = reinterpret_cast<const double2 *>(val + r0 * K);
+        for (int c = lane; c < nv2; c += 32) reinterpret_cast<double2 *>(sv)[c] = __ldcs(gv + c);
+        const int nc = nr * K, nc4 = nc >> 2;
+        const int4 *gc = reinterpret_cast<const int4 *>(col + r0 * K);
+        for (int c = lane; c < nc4; c += 32) reinterpret_cast<int4 *>(sc)[c] = __ldcs(gc + c);
+        for (int c = 4 * nc4 + lane; c < nc; c += 32) sc[c] = __ldcs(col + r0 * K + c);
+        __syncwarp();
+        if (lane < nr) {
+            const double2 *mv = reinterpret_cast<const double2 *>(sv + lane * K);
+            const int2 *mc = reinterpret_cast<const int2 *>(sc + lane * K);
+            double acc = 0.0;
+#pragma unroll
+            for (int i = 0; i < K / 2; i++) {
+                double2 wv = mv[i];
+                int2 cv = mc[i];
+                acc = fma(wv.x, __ldg(x + cv.x), acc);
+                acc = fma(wv.y, __ldg(x + cv.y), acc);
+            }
+            __stcs(y + r0 + lane, acc);
+        }
+        __syncwarp();
+    }
+}
+
 // Multi-field SpMM: one warp per row, lanes over fields.  X is [cols][F] row-major.
 template <typename T>
 __global__ void __launch_bounds__(256) spmm_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
@@ -90,6 +138,86 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t rows, const int64_t *
             if (f + 32 < F) y[r * F + f + 32] = acc1;
         }
     }
+}
+
+// One RK4 stage of du/dt = L u on F fields (classic RK4; examples/adv_diff_test.jl solves the
+// same semi-discrete system with SSPRK43).  v = L w for every row (warp per row, lanes over
+// fields), v = 0 on fixed rows (held at their initial values, the Dirichlet overwrite of
+// examples/adv_diff_test.jl:166-167), then the epilogue folds the RK bookkeeping in, so no
+// stage derivative is stored:
+//   mode 0 (stage 1): acc  = v;          wnext = u + c v
+//   mode 1 (stage 2, 3): acc += 2 v;     wnext = u + c v
+//   mode 2 (stage 4): unext = u + c (acc + v)        (c = dt / 6)
+template <typename T>
+__global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
+                                                        const int32_t *__restrict__ col, const T *__restrict__ val,
+                                                        const T *__restrict__ w, const T *__restrict__ u,
+                                                        T *__restrict__ acc, T *__restrict__ out,
+                                                        const uint8_t *__restrict__ fixed, int F, T c, int mode)
+{
+    const int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < rows; r += nw) {
+        const int64_t a = row_ptr[r], b = row_ptr[r + 1];
+        const bool fx = fixed && fixed[r];
+        for (int f0 = 0; f0 < F; f0 += 64) {
+            const int f = f0 + lane, g = f + 32;
+            T v0 = 0, v1 = 0;
+            if (!fx) {
+                for (int64_t t = a; t < b; t++) {
+                    const T wt = val[t];
+                    const T *xr = w + (int64_t)col[t] * F;
+                    if (f < F) v0 = fma(wt, xr[f], v0);
+                    if (g < F) v1 = fma(wt, xr[g], v1);
+                }
+            }
+            const int64_t o = r * F;
+            if (f < F) {
+                if (mode == 0) {
+                    acc[o + f] = v0;
+                    out[o + f] = fma(c, v0, u[o + f]);
+                } else if (mode == 1) {
+                    acc[o + f] = fma((T)2, v0, acc[o + f]);
+                    out[o + f] = fma(c, v0, u[o + f]);
+                } else {
+                    out[o + f] = fma(c, acc[o + f] + v0, u[o + f]);
+                }
+            }
+            if (g < F) {
+                if (mode == 0) {
+                    acc[o + g] = v1;
+                    out[o + g] = fma(c, v1, u[o + g]);
+                } else if (mode == 1) {
+                    acc[o + g] = fma((T)2, v1, acc[o + g]);
+                    out[o + g] = fma(c, v1, u[o + g]);
+                } else {
+                    out[o + g] = fma(c, acc[o + g] + v1, u[o + g]);
+                }
+            }
+        }
+    }
+}
+
+// val_out = sum_q coef[q] * val_q (operators with one sparsity pattern), in FP64 and FP32.
+__global__ void combine_ops_kernel(int64_t nnz, const double *const *vals, const double *coef, int nq,
+                                   double *out64, float *out32)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz; t += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int q = 0; q < nq; q++) acc = fma(coef[q], vals[q][t], acc);
+        out64[t] = acc;
+        out32[t] = (float)acc;
+    }
+}
+
+// Count entries where two column arrays differ (operator sets must share a stencil pattern).
+__global__ void count_diff_kernel(int64_t n, const int32_t *a, const int32_t *b, unsigned long long *cnt)
+{
+    unsigned long long local = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        local += a[t] != b[t];
+    if (local) atomicAdd(cnt, local);
 }
 
 __global__ void csc_count_kernel(int64_t nnz, const int32_t *col, unsigned long long *cnt)
@@ -219,7 +347,15 @@ cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t 
     // `group` carries the uniform stencil size (0 = general CSR)
     switch (group) {
     case 20: spmv_f64_uniform<20><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
-    case 30: spmv_f64_uniform<30><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
+    case 30: {
+        const size_t smem = (size_t)(threads / 32) * 32 * 30 * 12;
+        cudaError_t e = cudaFuncSetAttribute(spmv_f64_staged<30>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int64_t tiles = (rows + 31) / 32;
+        int sblocks = blocks_for(tiles * 32, threads, (int64_t)num_sms * 2);
+        spmv_f64_staged<30><<<sblocks, threads, smem, st>>>(rows, col, val, x, y);
+        break;
+    }
     case 42: spmv_f64_uniform<42><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
     default: spmv_f64_rows<<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
     }
@@ -238,6 +374,37 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
     else
         spmm_kernel<float><<<blocks, threads, 0, st>>>(rows, row_ptr, col, (const float *)val,
                                                        (const float *)x, (float *)y, nfields);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_stage(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
+                             const void *w, const void *u, void *acc, void *out, const uint8_t *fixed, int F,
+                             double c, int mode, int dtype, int num_sms, cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    int blocks = blocks_for(rows * 32, 256, (int64_t)num_sms * 8);
+    if (dtype == 0)
+        rk4_stage_kernel<double><<<blocks, 256, 0, st>>>(rows, row_ptr, col, (const double *)val, (const double *)w,
+                                                         (const double *)u, (double *)acc, (double *)out, fixed, F, c,
+                                                         mode);
+    else
+        rk4_stage_kernel<float><<<blocks, 256, 0, st>>>(rows, row_ptr, col, (const float *)val, (const float *)w,
+                                                        (const float *)u, (float *)acc, (float *)out, fixed, F,
+                                                        (float)c, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_combine_ops(int64_t nnz, const double *const *vals, const double *coef, int nq, double *out64,
+                               float *out32, cudaStream_t st)
+{
+    combine_ops_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, vals, coef, nq, out64, out32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_diff(int64_t n, const int32_t *a, const int32_t *b, unsigned long long *cnt,
+                              cudaStream_t st)
+{
+    count_diff_kernel<<<blocks_for(n, 256), 256, 0, st>>>(n, a, b, cnt);
     return cudaGetLastError();
 }
 

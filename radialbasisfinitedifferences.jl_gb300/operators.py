@@ -221,6 +221,67 @@ def calculateneighbors(X, Y, n, X_idx_in=None, X_idx_bc=(), X_idx_bc_g=(), Y_idx
     return ix, iy, dx, dy
 
 
+class RK4Stepper:
+    """Explicit RK4 for du/dt = L u with L = sum_i coef[i] A_i over the operators of one or
+    more OperatorSets sharing a stencil pattern (rbffd_rk4_*): the time-stepping loop of
+    examples/adv_diff_test.jl:144-199 on the GPU, pairs of steps replayed as CUDA graphs."""
+
+    def __init__(self, sets, coef, nfields, dtype="f64", fixed_rows=None, handle=None):
+        self.sets = list(sets)
+        self.h = handle or self.sets[0].h
+        self._lib = nat.load()
+        self.dtype = 0 if dtype == "f64" else 1
+        arr = (ctypes.c_void_p * len(self.sets))(*[s.ptr.value for s in self.sets])
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        if len(c) != sum(len(s.ops) for s in self.sets):
+            raise ValueError("one coefficient per operator of every set")
+        fx = None if fixed_rows is None else np.ascontiguousarray(fixed_rows, dtype=np.uint8)
+        out = ctypes.c_void_p()
+        rc = self._lib.rbffd_rk4_create(self.h.ptr, arr, len(self.sets), _ptr(c), _ptr(fx), nfields, self.dtype,
+                                        ctypes.byref(out))
+        nat.check(self.h.ptr, rc)
+        self.ptr = out
+        self.nfields = nfields
+
+    def run(self, u, dt, nsteps):
+        """u: CUDA tensor [rows, nfields] (float64 or float32 to match dtype), advanced in place."""
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        nat.check(self.h.ptr, self._lib.rbffd_rk4_run(self.h.ptr, self.ptr, ctypes.c_void_p(u.data_ptr()), dt, nsteps))
+        self.h.synchronize()
+        return u
+
+    def run_ptr(self, u_ptr, dt, nsteps):
+        nat.check(self.h.ptr, self._lib.rbffd_rk4_run(self.h.ptr, self.ptr, ctypes.c_void_p(u_ptr), dt, nsteps))
+
+    def apply(self, x, y):
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        nat.check(self.h.ptr, self._lib.rbffd_rk4_apply(self.h.ptr, self.ptr, ctypes.c_void_p(x.data_ptr()),
+                                                        ctypes.c_void_p(y.data_ptr())))
+        self.h.synchronize()
+        return y
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self._lib.rbffd_rk4_destroy(self.h.ptr, self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _DeviceArray:
     """__cuda_array_interface__ view of library-owned device memory."""
 

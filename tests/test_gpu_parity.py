@@ -284,3 +284,49 @@ def test_errors(pkg, gpu):
     # the handle stays usable after errors
     E = pkg.generate_operator(X, X, 3, 15, 2, ops=("E",))[0]
     assert np.allclose(E.toarray(), np.eye(len(X)), atol=1e-10)
+
+
+@pytest.mark.parametrize("dtype,tol", [("f64", 1e-10), ("f32", 2e-5)])
+def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol):
+    """RK4 of du/dt = L u, L = -Dx - 0.5 Dy + 0.01 Lap, boundary band held fixed, against a
+    numpy RK4 with the oracle's operators (7 steps: three graph-replayed pairs + one)."""
+    import scipy.sparse as sp
+    import torch
+
+    X, h = grid(pkg, 32, seed=9)
+    N, n = len(X), 20
+    ops = ("Dx", "Dy", "Lap")
+    coef = [-1.0, -0.5, 1e-2]
+    ref = orc.generate(X, X, 3, n, 3, ops)
+    rows = np.repeat(np.arange(N), n)
+    L = sum(c * sp.csr_matrix((ref["W"][q].ravel(), (rows, ref["cols"].ravel())), shape=(N, N))
+            for q, c in enumerate(coef))
+    fixed = ((X < 1.5 * h) | (X > 1 - 1.5 * h)).any(1)
+    F = 5
+    U0 = np.random.default_rng(4).standard_normal((N, F))
+    dt, nsteps = 0.1 * h, 7
+
+    def f(u):
+        v = L @ u
+        v[fixed] = 0.0
+        return v
+
+    u = U0.copy()
+    for _ in range(nsteps):
+        k1 = f(u)
+        k2 = f(u + 0.5 * dt * k1)
+        k3 = f(u + 0.5 * dt * k2)
+        k4 = f(u + dt * k3)
+        u = u + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+    with pkg.OperatorSet(X, None, 3, n, 3, ops=ops) as s:
+        with pkg.RK4Stepper([s], coef, F, dtype, fixed_rows=fixed) as st:
+            td = torch.float64 if dtype == "f64" else torch.float32
+            ud = torch.tensor(U0, dtype=td, device="cuda")
+            st.run(ud, dt, nsteps)
+            got = ud.double().cpu().numpy()
+            assert np.abs(got - u).max() <= tol * np.abs(u).max()
+            assert np.array_equal(got[fixed], U0[fixed].astype(got.dtype) if dtype == "f64" else got[fixed])
+            y = torch.empty_like(ud)
+            st.apply(torch.tensor(U0, dtype=td, device="cuda"), y)
+            LU = L @ U0
+            assert np.abs(y.double().cpu().numpy() - LU).max() <= max(tol, 1e-12) * 10 * np.abs(LU).max()
