@@ -1,0 +1,875 @@
+// Mixed-precision weight solves: FP32 preconditioner built from the Schur complement of the
+// saddle system, FP64 residuals, iterative refinement.  One warp per local system.
+//
+// The local system of src/generate_operator.jl (rbfblock/polynomialblock) is
+//   A = [Phi P; P' 0],  Phi_ij = phi(|x_i - x_j|) (n x n),  P_il = monomial l at x_i (n x m).
+// Its FP32 inverse is never formed.  The kernel keeps
+//   * Phi^-1 in registers: lane l holds the Gauss-Jordan result for row l (and l + 32), so an
+//     elimination step is a run of independent FMAs on compile-time register indices and only
+//     the pivot row travels through shared memory;
+//   * G = Phi^-1 P (n x m) and Sinv = S^-1, S = -P' G (m x m), in shared memory.
+// A correction A^-1 [r1; r2] = [w; lambda] is then
+//   lambda = Sinv (r2 - G' r1),   w = Phi^-1 r1 - G lambda,
+// i.e. one register matvec plus three short shared-memory matvecs.  Refinement x += A^-1 (b - A x)
+// runs with FP64 residuals (Phi packed as its lower triangle, P, x and b in FP64) until the
+// estimated relative error of the weights rho * |dx| / |x| is below refine_tol; a system that
+// stalls (rho > 1/2), meets a zero pivot or produces a non-finite value goes to the FP64
+// fallback queue, as in the shared-memory mixed kernel of weights.cu.
+//
+// FP64 instructions are the scarce resource (1/64 of the FP32 rate), so every FP64 instruction
+// works on lane-parallel data, conversions between float and double use the integer pipe, and
+// maxima and comparisons use integer keys.
+//
+// Pivoting is virtual: rows never move.  ps[i] is the step at which row i was the pivot and
+// perm[c] the pivot row of step c; the Gauss-Jordan result B then satisfies
+// inv(M)[ps[i]][perm[j]] = B[i][j].
+#pragma once
+
+#include <type_traits>
+
+#include "solve_common.cuh"
+
+namespace {
+
+constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never updated
+
+// Resident CTAs of 4 warps per SM requested for stencils of <= 32 nodes (4: <= 128 registers
+// per thread, 16 warps per SM).
+#ifndef RBFFD_SCHUR_MIN_BLOCKS
+#define RBFFD_SCHUR_MIN_BLOCKS 4
+#endif
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F &&f)
+{
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
+// Select a (c true) or b in one PTX instruction, so that a chain of slot selects is not folded
+// back into a dynamically indexed register array (which would live in local memory).
+__device__ __forceinline__ float sel_f32(bool c, float a, float b)
+{
+    float r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.s32 p, %3, 0;\n\tselp.f32 %0, %1, %2, p;\n\t}"
+        : "=f"(r)
+        : "f"(a), "f"(b), "r"((int)c));
+    return r;
+}
+
+// float -> double from the IEEE-754 bit fields (exact for normal numbers; subnormals flush to
+// a signed zero; inf and NaN are kept).
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    unsigned u = __float_as_uint(f);
+    unsigned e = (u >> 23) & 0xffu;
+    unsigned sign = u & 0x80000000u;
+    unsigned mant = u & 0x7fffffu;
+    unsigned e64 = e == 255u ? 2047u : e + (1023u - 127u);
+    unsigned hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
+    unsigned lo = e == 0u ? 0u : (mant << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float by truncation of the mantissa (|error| < 1 ulp of float), from the bit
+// fields.  Magnitudes above the float range give inf, below the normal range a signed zero;
+// NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32(double d)
+{
+    unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    unsigned sign = hi & 0x80000000u;
+    int e = (int)((hi >> 20) & 0x7ffu);
+    int e32 = e - 1023 + 127;
+    unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned out;
+    if (e == 2047)
+        out = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
+    else if (e32 >= 255)
+        out = sign | 0x7f800000u;
+    else if (e32 <= 0)
+        out = sign;
+    else
+        out = sign | ((unsigned)e32 << 23) | mant;
+    return __uint_as_float(out);
+}
+
+// sqrt(a) for a positive normal double, without a library call: an FP32 reciprocal square
+// root of the mantissa (exponent split off on the integer pipe, a = a' 4^k with a' in [1, 4))
+// seeds Heron's iteration s <- s + (a - s^2) / (2 s), with 1 / (2 s) taken from the seed;
+// the error goes 2^-22 -> 2^-44 -> below FP64 rounding.  y0 returns the seed (~1/sqrt(a)).
+__device__ __forceinline__ double sqrt_nr(double a, double &y0)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const int ex = (int)((hi >> 20) & 0x7ffu) - 1023;
+    const int k = ex >> 1;  // floor(ex / 2)
+    const unsigned fb = ((unsigned)(ex - 2 * k + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const float yf = rsqrtf(__uint_as_float(fb));
+    const double yd = f32_to_f64(yf);
+    y0 = __hiloint2double(__double2hiint(yd) - k * (1 << 20), __double2loint(yd));  // yf 2^-k
+    const double h = __hiloint2double(__double2hiint(y0) - (1 << 20), __double2loint(y0));  // y0 / 2
+    double s = a * y0;
+    s = fma(fma(-s, s, a), h, s);
+    return fma(fma(-s, s, a), h, s);
+}
+
+// 1/s from a seed y0 ~ 1/s (relative error ~2^-22) by two Newton-Raphson steps
+// y <- y + y (1 - s y).
+__device__ __forceinline__ double recip_nr(double s, double y0)
+{
+    double y = fma(y0, fma(-s, y0, 1.0), y0);
+    return fma(y, fma(-s, y, 1.0), y);
+}
+
+// phi = r^p from r^2 without library calls (r^2 = 0 gives 0).
+__device__ __forceinline__ double phi64_nr(double r2, int p)
+{
+    double v = r2;
+    for (int i = 1; i < (p >> 1); i++) v *= r2;
+    if (p < 2) v = 1.0;
+    if (p & 1) {
+        double y0;
+        const double rt = sqrt_nr(r2, y0);
+        v *= rt;
+    }
+    return r2 > 0.0 ? v : 0.0;
+}
+
+template <int S>
+struct RegRows {
+    static constexpr int NS = (S + 31) / 32;
+    float a[NS][S];
+    int ps[NS];
+};
+
+// Per-warp shared-memory carve-up.  The setup-only arrays (x32, P32, Pp, Sm) share storage
+// with the refinement arrays (B, X, R32, U, Lam, bp).
+struct SchurLayout {
+    size_t phi, P, xs, sid, G, Sinv, permP, dinvP, permS, dinvS, prow, sc;
+    size_t x32, P32, Pp, Sm;
+    size_t B, X, R32, U, Lam, bp;
+    size_t total;
+    int ldg, lds;
+};
+
+__host__ __device__ inline SchurLayout make_schur_layout(int SP, int SM, int max_n, int max_m, int nops)
+{
+    SchurLayout L;
+    const int n4 = (max_n + 3) & ~3, s = max_n + max_m, rq = (nops + 3) / 4;
+    const int wmax = SP > SM ? SP : SM;
+    L.ldg = max_m | 1;
+    L.lds = max_m | 1;
+    size_t o = 0;
+    L.phi = o;
+    o += al16(sizeof(double) * (size_t)max_n * (max_n + 1) / 2);
+    L.P = o;
+    o += al16(sizeof(double) * max_n * max_m);
+    L.xs = o;
+    o += al16(sizeof(double) * 2 * max_n);
+    L.sid = o;
+    o += al16(sizeof(int) * max_n);
+    L.G = o;
+    o += al16(sizeof(float) * max_n * L.ldg);
+    L.Sinv = o;
+    o += al16(sizeof(float) * max_m * L.lds);
+    L.permP = o;
+    o += al16(sizeof(int) * SP);
+    L.dinvP = o;
+    o += al16(sizeof(float) * SP);
+    L.permS = o;
+    o += al16(sizeof(int) * SM);
+    L.dinvS = o;
+    o += al16(sizeof(float) * SM);
+    L.prow = o;
+    o += al16(sizeof(float) * (wmax + 4));
+    L.sc = o;
+    o += al16(sizeof(double) * 2 * nops);
+    // union: setup arrays
+    size_t u = o;
+    L.x32 = u;
+    u += al16(sizeof(float2) * max_n);
+    L.P32 = u;
+    u += al16(sizeof(float) * max_n * max_m);
+    L.Pp = u;
+    u += al16(sizeof(float) * max_m * n4);
+    L.Sm = u;
+    u += al16(sizeof(float) * max_m * max_m);
+    // union: refinement arrays
+    size_t v = o;
+    L.B = v;
+    v += al16(sizeof(double) * s * nops);
+    L.X = v;
+    v += al16(sizeof(double) * s * nops);
+    L.R32 = v;
+    v += al16(sizeof(float) * s * nops);
+    L.U = v;
+    v += al16(sizeof(float) * max_m * nops);
+    L.Lam = v;
+    v += al16(sizeof(float4) * max_m * rq);
+    L.bp = v;
+    v += al16(sizeof(float4) * max_n * rq);
+    L.total = u > v ? u : v;
+    return L;
+}
+
+// Phi rows in FP32 straight into registers: row i = lane + 32 k, column j compile-time.
+template <int SP>
+__device__ __forceinline__ void fill_phi_rows(RegRows<SP> &R, const float2 *x32, int n, int p, int lane)
+{
+    static_for<0, RegRows<SP>::NS>([&](auto KK) {
+        constexpr int k = decltype(KK)::value;
+        const int i = lane + 32 * k;
+        const bool act = i < n;
+        R.ps[k] = act ? NOTYET : PADROW;
+        float2 xi = x32[act ? i : 0];
+        static_for<0, SP>([&](auto JJ) {
+            constexpr int j = decltype(JJ)::value;
+            float v = 0.0f;
+            if (j < n) {
+                float2 xj = x32[j];
+                float dx = xi.x - xj.x, dy = xi.y - xj.y;
+                v = act ? phi32(fmaf(dx, dx, dy * dy), p) : 0.0f;
+            }
+            R.a[k][j] = v;
+        });
+    });
+}
+
+// In-place Gauss-Jordan inversion of the s x s leading block in registers with virtual partial
+// pivoting.  Step c picks the pivot among rows not yet used (largest |a[c]|, lowest row on
+// ties: a redux.sync max over the |a| bit patterns, then a redux.sync min over row ids),
+// publishes it through shared memory and eliminates column c from every other row.  A pivot
+// row stays multiplied by its pivot (elimination is linear, so later updates apply unchanged)
+// and is divided by it once at the end, so each step is a uniform FMA sweep.  Fails on a
+// zero, subnormal, infinite or NaN pivot.
+template <int S>
+__device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *dinv, float *prow, int lane)
+{
+    constexpr int NS = RegRows<S>::NS;
+    bool ok = true;
+    static_for<0, S>([&](auto CC) {
+        constexpr int c = decltype(CC)::value;
+        if (c >= s || !ok) return;
+        unsigned key = 0u;
+        int brow = INT_MAX;
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            unsigned kk = __float_as_uint(R.a[k][c]) & 0x7fffffffu;
+            if (R.ps[k] == NOTYET && kk > key) {
+                key = kk;
+                brow = lane + 32 * k;
+            }
+        }
+        unsigned mk = __reduce_max_sync(RBFFD_FULL, key);
+        if (mk < 0x00800000u || mk >= 0x7f800000u) {
+            ok = false;
+            return;
+        }
+        int bi = (int)__reduce_min_sync(RBFFD_FULL, (unsigned)(key == mk ? brow : INT_MAX));
+        if (lane == (bi & 31)) {
+            const int oslot = bi >> 5;
+#pragma unroll
+            for (int j4 = 0; j4 < (S + 3) / 4; j4++) {
+                float e[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int j = 4 * j4 + u;
+                    float v = 0.0f;
+                    if (j < S) {
+                        v = R.a[0][j];
+#pragma unroll
+                        for (int k = 1; k < NS; k++) v = sel_f32(oslot == k, R.a[k][j], v);
+                    }
+                    e[u] = v;
+                }
+                reinterpret_cast<float4 *>(prow)[j4] = make_float4(e[0], e[1], e[2], e[3]);
+            }
+        }
+        if (lane == 0) perm[c] = bi;
+        __syncwarp();
+        const float inv = __fdividef(1.0f, prow[c]);
+        if (lane == 0) dinv[c] = inv;
+        float fs[NS];
+        bool piv[NS];
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            piv[k] = (lane + 32 * k == bi);
+            const bool elim = R.ps[k] != PADROW && !piv[k];
+            fs[k] = elim ? R.a[k][c] * inv : 0.0f;
+            if (piv[k]) R.ps[k] = c;
+        }
+#pragma unroll
+        for (int j4 = 0; j4 < (S + 3) / 4; j4++) {
+            const float4 pv = reinterpret_cast<const float4 *>(prow)[j4];
+            const float pj[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = 4 * j4 + u;
+                if (j < S && j != c) {
+#pragma unroll
+                    for (int k = 0; k < NS; k++) R.a[k][j] = fmaf(-fs[k], pj[u], R.a[k][j]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            if (R.ps[k] != PADROW) R.a[k][c] = piv[k] ? 1.0f : -fs[k];
+        }
+        __syncwarp();
+    });
+    if (ok) {
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            const float d = (R.ps[k] >= 0 && R.ps[k] < s) ? dinv[R.ps[k]] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < S; j++) R.a[k][j] *= d;
+        }
+    }
+    return ok;
+}
+
+// G = Phi^-1 P, S = -P' G, Sinv = S^-1 (natural order).  Returns false on a singular S.
+template <int SP, int SM>
+__device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m, const int *permP, const float *P32,
+                                            float *Pp, float *G, int ldg, float *Sm, float *Sinv, int lds,
+                                            int *permS, float *dinvS, float *prow, int lane)
+{
+    constexpr int NS = RegRows<SP>::NS;
+    const int n4 = (n + 3) & ~3;
+    for (int t = lane; t < m * n4; t += 32) {
+        const int l = t / n4, jj = t - l * n4;
+        Pp[t] = jj < n ? P32[permP[jj] * m + l] : 0.0f;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        if (32 * k >= n) break;
+        const int v = RP.ps[k];
+        const bool own = v >= 0 && v < n;
+        for (int l = 0; l < m; l += 2) {
+            const int l1 = l + 1 < m ? l + 1 : l;
+            const float4 *p0 = reinterpret_cast<const float4 *>(Pp + l * n4);
+            const float4 *p1 = reinterpret_cast<const float4 *>(Pp + l1 * n4);
+            float a0 = 0.0f, a1 = 0.0f, b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+            for (int j4 = 0; j4 < SP / 4; j4 += 2) {
+                if (4 * j4 < n) {
+                    const float4 w = p0[j4], z = p1[j4];
+                    a0 = fmaf(RP.a[k][4 * j4 + 0], w.x, a0);
+                    b0 = fmaf(RP.a[k][4 * j4 + 0], z.x, b0);
+                    a0 = fmaf(RP.a[k][4 * j4 + 1], w.y, a0);
+                    b0 = fmaf(RP.a[k][4 * j4 + 1], z.y, b0);
+                    a0 = fmaf(RP.a[k][4 * j4 + 2], w.z, a0);
+                    b0 = fmaf(RP.a[k][4 * j4 + 2], z.z, b0);
+                    a0 = fmaf(RP.a[k][4 * j4 + 3], w.w, a0);
+                    b0 = fmaf(RP.a[k][4 * j4 + 3], z.w, b0);
+                }
+                if (4 * j4 + 4 < n) {
+                    const float4 w = p0[j4 + 1], z = p1[j4 + 1];
+                    a1 = fmaf(RP.a[k][4 * j4 + 4], w.x, a1);
+                    b1 = fmaf(RP.a[k][4 * j4 + 4], z.x, b1);
+                    a1 = fmaf(RP.a[k][4 * j4 + 5], w.y, a1);
+                    b1 = fmaf(RP.a[k][4 * j4 + 5], z.y, b1);
+                    a1 = fmaf(RP.a[k][4 * j4 + 6], w.z, a1);
+                    b1 = fmaf(RP.a[k][4 * j4 + 6], z.z, b1);
+                    a1 = fmaf(RP.a[k][4 * j4 + 7], w.w, a1);
+                    b1 = fmaf(RP.a[k][4 * j4 + 7], z.w, b1);
+                }
+            }
+            if (own) {
+                G[v * ldg + l] = a0 + a1;
+                if (l + 1 < m) G[v * ldg + l + 1] = b0 + b1;
+            }
+        }
+    }
+    __syncwarp();
+    for (int t = lane; t < m * m; t += 32) {
+        const int aa = t / m, bb = t - aa * m;
+        float s0 = 0.0f, s1 = 0.0f;
+        int i = 0;
+        for (; i + 2 <= n; i += 2) {
+            s0 = fmaf(P32[i * m + aa], G[i * ldg + bb], s0);
+            s1 = fmaf(P32[(i + 1) * m + aa], G[(i + 1) * ldg + bb], s1);
+        }
+        if (i < n) s0 = fmaf(P32[i * m + aa], G[i * ldg + bb], s0);
+        Sm[t] = -(s0 + s1);
+    }
+    __syncwarp();
+    RegRows<SM> RS;
+    {
+        const bool act = lane < m;
+        RS.ps[0] = act ? NOTYET : PADROW;
+        static_for<0, SM>([&](auto BB) {
+            constexpr int b = decltype(BB)::value;
+            float v = 0.0f;
+            if (act && b < m) v = Sm[lane * m + b];
+            RS.a[0][b] = v;
+        });
+    }
+    __syncwarp();
+    const bool ok = reg_gj<SM>(RS, m, permS, dinvS, prow, lane);
+    if (ok) {
+        const int v = RS.ps[0];
+        if (v >= 0 && v < m) {
+            static_for<0, SM>([&](auto BB) {
+                constexpr int b = decltype(BB)::value;
+                if (b < m) Sinv[v * lds + permS[b]] = RS.a[0][b];
+            });
+        }
+    }
+    __syncwarp();
+    return ok;
+}
+
+// R32 <- A^-1 R32 (s x r, row-major) through Phi^-1 (registers), G and Sinv.
+template <int SP, int RMAX>
+__device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int m, int r, const int *permP,
+                                              const float *G, int ldg, const float *Sinv, int lds, float *R32,
+                                              float *U, float *Lam, float4 *bp, int lane)
+{
+    constexpr int NS = RegRows<SP>::NS;
+    constexpr int RQ = (RMAX + 3) / 4;
+    // (1) permuted r1 rows as float4 groups; u = r2 - G' r1
+    for (int t = lane; t < n * RQ; t += 32) {
+        const int jj = t / RQ, g = t - jj * RQ;
+        const float *src = R32 + permP[jj] * r;
+        float e[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) e[u] = (4 * g + u < r) ? src[4 * g + u] : 0.0f;
+        bp[t] = make_float4(e[0], e[1], e[2], e[3]);
+    }
+    for (int e = lane; e < m * r; e += 32) {
+        const int l = e / r, q = e - l * r;
+        float u0 = R32[(n + l) * r + q], u1 = 0.0f;
+        int i = 0;
+        for (; i + 2 <= n; i += 2) {
+            u0 = fmaf(-G[i * ldg + l], R32[i * r + q], u0);
+            u1 = fmaf(-G[(i + 1) * ldg + l], R32[(i + 1) * r + q], u1);
+        }
+        if (i < n) u0 = fmaf(-G[i * ldg + l], R32[i * r + q], u0);
+        U[e] = u0 + u1;
+    }
+    __syncwarp();
+    // (2) lambda = Sinv u (shared memory); t = Phi^-1 r1 (registers)
+    for (int e = lane; e < m * r; e += 32) {
+        const int l = e / r, q = e - l * r;
+        float v0 = 0.0f, v1 = 0.0f;
+        int aa = 0;
+        for (; aa + 2 <= m; aa += 2) {
+            v0 = fmaf(Sinv[l * lds + aa], U[aa * r + q], v0);
+            v1 = fmaf(Sinv[l * lds + aa + 1], U[(aa + 1) * r + q], v1);
+        }
+        if (aa < m) v0 = fmaf(Sinv[l * lds + aa], U[aa * r + q], v0);
+        Lam[l * 4 * RQ + q] = v0 + v1;
+    }
+    float acc[NS][4 * RQ];
+#pragma unroll
+    for (int k = 0; k < NS; k++)
+#pragma unroll
+        for (int q = 0; q < 4 * RQ; q++) acc[k][q] = 0.0f;
+#pragma unroll
+    for (int jj = 0; jj < SP; jj++) {
+        if (jj < n) {
+#pragma unroll
+            for (int g = 0; g < RQ; g++) {
+                const float4 v = bp[jj * RQ + g];
+#pragma unroll
+                for (int k = 0; k < NS; k++) {
+                    acc[k][4 * g + 0] = fmaf(RP.a[k][jj], v.x, acc[k][4 * g + 0]);
+                    acc[k][4 * g + 1] = fmaf(RP.a[k][jj], v.y, acc[k][4 * g + 1]);
+                    acc[k][4 * g + 2] = fmaf(RP.a[k][jj], v.z, acc[k][4 * g + 2]);
+                    acc[k][4 * g + 3] = fmaf(RP.a[k][jj], v.w, acc[k][4 * g + 3]);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    // (3) w = t - G lambda
+    const float4 *Lam4 = reinterpret_cast<const float4 *>(Lam);
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        const int v = RP.ps[k];
+        const bool own = v >= 0 && v < n;
+        const int vv = own ? v : 0;
+        for (int l = 0; l < m; l++) {
+            const float gv = G[vv * ldg + l];
+#pragma unroll
+            for (int g = 0; g < RQ; g++) {
+                const float4 lm = Lam4[l * RQ + g];
+                acc[k][4 * g + 0] = fmaf(-gv, lm.x, acc[k][4 * g + 0]);
+                acc[k][4 * g + 1] = fmaf(-gv, lm.y, acc[k][4 * g + 1]);
+                acc[k][4 * g + 2] = fmaf(-gv, lm.z, acc[k][4 * g + 2]);
+                acc[k][4 * g + 3] = fmaf(-gv, lm.w, acc[k][4 * g + 3]);
+            }
+        }
+        if (own) {
+#pragma unroll
+            for (int q = 0; q < RMAX; q++)
+                if (q < r) R32[v * r + q] = acc[k][q];
+        }
+    }
+    for (int e = lane; e < m * r; e += 32) {
+        const int l = e / r, q = e - l * r;
+        R32[(n + l) * r + q] = Lam[l * 4 * RQ + q];
+    }
+    __syncwarp();
+}
+
+// Phi lower triangle (with its zero diagonal) packed by rows: element (i, j <= i) at
+// i (i + 1) / 2 + j.
+__device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
+
+// R32 <- float(B - A X) with FP64 products: Phi rows lane-per-row (all operators of a row per
+// lane, so each Phi element is loaded once), P' rows lane-per-element.
+template <int SP, int RMAX>
+__device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r,
+                                              const double *B, const double *X, float *R32, int lane)
+{
+    constexpr int NS = SP / 32;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        if (32 * k >= n) break;
+        const int i = lane + 32 * k;
+        const bool act = i < n;
+        const int ii = act ? i : n - 1;
+        double a0[RMAX], a1[RMAX];
+#pragma unroll
+        for (int q = 0; q < RMAX; q++) {
+            a0[q] = 0.0;
+            a1[q] = 0.0;
+            if (q < r) a0[q] = B[ii * r + q];
+        }
+        const int offi = tri_off(ii);
+        int offj = 0;  // tri_off(jj)
+        int jj = 0;
+        for (; jj + 2 <= n; jj += 2) {
+            const int ad0 = jj <= ii ? offi + jj : offj + ii;
+            offj += jj + 1;
+            const int ad1 = jj + 1 <= ii ? offi + jj + 1 : offj + ii;
+            offj += jj + 2;
+            const double f0 = phiP[ad0], f1 = phiP[ad1];
+            const double *x0 = X + jj * r;
+#pragma unroll
+            for (int q = 0; q < RMAX; q++) {
+                if (q < r) {
+                    a0[q] = fma(-f0, x0[q], a0[q]);
+                    a1[q] = fma(-f1, x0[r + q], a1[q]);
+                }
+            }
+        }
+        if (jj < n) {
+            const int ad0 = jj <= ii ? offi + jj : offj + ii;
+            const double f0 = phiP[ad0];
+#pragma unroll
+            for (int q = 0; q < RMAX; q++)
+                if (q < r) a0[q] = fma(-f0, X[jj * r + q], a0[q]);
+        }
+        const double *Pi = P + ii * m;
+        const double *Xl = X + n * r;
+        int l = 0;
+        for (; l + 2 <= m; l += 2) {
+            const double p0 = Pi[l], p1 = Pi[l + 1];
+#pragma unroll
+            for (int q = 0; q < RMAX; q++) {
+                if (q < r) {
+                    a0[q] = fma(-p0, Xl[l * r + q], a0[q]);
+                    a1[q] = fma(-p1, Xl[(l + 1) * r + q], a1[q]);
+                }
+            }
+        }
+        if (l < m) {
+            const double p0 = Pi[l];
+#pragma unroll
+            for (int q = 0; q < RMAX; q++)
+                if (q < r) a0[q] = fma(-p0, Xl[l * r + q], a0[q]);
+        }
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RMAX; q++)
+                if (q < r) R32[i * r + q] = f64_to_f32(a0[q] + a1[q]);
+        }
+    }
+    for (int e = lane; e < m * r; e += 32) {
+        const int l = e / r, q = e - l * r;
+        double a0 = B[(n + l) * r + q], a1 = 0.0;
+        int jj = 0;
+        for (; jj + 2 <= n; jj += 2) {
+            a0 = fma(-P[jj * m + l], X[jj * r + q], a0);
+            a1 = fma(-P[(jj + 1) * m + l], X[(jj + 1) * r + q], a1);
+        }
+        if (jj < n) a0 = fma(-P[jj * m + l], X[jj * r + q], a0);
+        R32[(n + l) * r + q] = f64_to_f32(a0 + a1);
+    }
+    __syncwarp();
+}
+
+// Packed FP64 Phi (two pairs per lane per pass) and FP64 P rows.
+__device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
+                                                    double *P, int lane)
+{
+    const int npairs = n * (n - 1) / 2;  // strictly lower pairs, row-major: t = i (i - 1) / 2 + j
+    for (int t = lane; t < npairs; t += 64) {
+        const int t2 = t + 32;
+        const bool two = t2 < npairs;
+        int i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)t)) * 0.5f);
+        if ((i * (i - 1)) / 2 > t) i--;
+        if (((i + 1) * i) / 2 <= t) i++;
+        const int j = t - (i * (i - 1)) / 2;
+        const int tt = two ? t2 : t;
+        int i2 = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)tt)) * 0.5f);
+        if ((i2 * (i2 - 1)) / 2 > tt) i2--;
+        if (((i2 + 1) * i2) / 2 <= tt) i2++;
+        const int j2 = tt - (i2 * (i2 - 1)) / 2;
+        const double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
+        const double dx2 = xs[2 * i2] - xs[2 * j2], dy2 = xs[2 * i2 + 1] - xs[2 * j2 + 1];
+        const double v = phi64_nr(fma(dx, dx, dy * dy), p);
+        const double v2 = phi64_nr(fma(dx2, dx2, dy2 * dy2), p);
+        phiP[t + i] = v;  // tri_off(i) + j = t + i
+        if (two) phiP[tt + i2] = v2;
+    }
+    for (int i = lane; i < n; i += 32) {
+        phiP[tri_off(i) + i] = 0.0;
+        monomial_row<double>(xs[2 * i], xs[2 * i + 1], deg, P + i * m, 1);
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ int ifact(int e)
+{
+    int c = 1;
+    for (int t = 2; t <= e; t++) c *= t;
+    return c;
+}
+
+// Right-hand sides of one evaluation point y~ (scaled coordinates) into B (s x r).  Same
+// formulas as build_rhs, with r and 1/r from sqrt_nr / recip_nr, per-system scale factors sc[2 q + c] = sx^a sy^b precomputed, and the polynomial rows
+// of a point at the stencil centre (y~ = 0: the common collocated case) from integers.
+__device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double *xs, int n, int m, double yx,
+                                                double yy, const double *sc, bool need_rinv, double *B, int lane)
+{
+    const int r = ops.nops;
+    for (int i = lane; i < n; i += 32) {
+        double cx = yx - xs[2 * i], cy = yy - xs[2 * i + 1];
+        if (is_zero64(cx)) cx = EPS64;
+        if (is_zero64(cy)) cy = EPS64;
+        const double r2 = fma(cx, cx, cy * cy);
+        double y0;
+        const double rr = sqrt_nr(r2, y0);
+        const double rinv = need_rinv ? recip_nr(rr, y0) : 0.0;
+        for (int q = 0; q < r; q++) {
+            const OpDesc &od = ops.op[q];
+            double v = 0.0;
+            for (int cidx = 0; cidx < od.ncomp; cidx++) {
+                const OpComp &oc = od.c[cidx];
+                double cv = 0.0;
+                for (int t = 0; t < oc.nterm; t++) {
+                    const RbfTerm &tm = oc.t[t];
+                    double tv = tm.coef;
+                    for (int e = 0; e < tm.ex; e++) tv *= cx;
+                    for (int e = 0; e < tm.ey; e++) tv *= cy;
+                    if (tm.er >= 0)
+                        for (int e = 0; e < tm.er; e++) tv *= rr;
+                    else
+                        for (int e = 0; e < -tm.er; e++) tv *= rinv;
+                    cv += tv;
+                }
+                if (od.ncomp > 1) cv *= sc[2 * q + cidx];
+                v += cv;
+            }
+            B[i * r + q] = v;
+        }
+    }
+    const bool at0 = is_zero64(yx) && is_zero64(yy);
+    for (int l = lane; l < m; l += 32) {
+        int t = 0, rem = l;
+        while (rem > t) {
+            rem -= t + 1;
+            t++;
+        }
+        const int ea = t - rem, eb = rem;
+        for (int q = 0; q < r; q++) {
+            const OpDesc &od = ops.op[q];
+            double v = 0.0;
+            for (int cidx = 0; cidx < od.ncomp; cidx++) {
+                const OpComp &oc = od.c[cidx];
+                if (oc.a > ea || oc.b > eb) continue;
+                double cv;
+                if (at0) {
+                    if (oc.a != ea || oc.b != eb) continue;
+                    cv = f32_to_f64((float)(ifact(ea) * ifact(eb)));
+                } else {
+                    cv = falling(ea, oc.a) * falling(eb, oc.b) * ipow(yx, ea - oc.a) * ipow(yy, eb - oc.b);
+                }
+                if (od.ncomp > 1) cv *= sc[2 * q + cidx];
+                v += cv;
+            }
+            B[(n + l) * r + q] = v;
+        }
+    }
+    __syncwarp();
+}
+
+template <int SP, int SM, int RMAX>
+__global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const SchurLayout L = make_schur_layout(SP, SM, a.max_n, a.max_m, ops.nops);
+    unsigned char *base = smem_raw + (size_t)wib * L.total;
+    double *phiP = (double *)(base + L.phi);
+    double *P = (double *)(base + L.P);
+    double *xs = (double *)(base + L.xs);
+    int *sid = (int *)(base + L.sid);
+    float *G = (float *)(base + L.G);
+    float *Sinv = (float *)(base + L.Sinv);
+    int *permP = (int *)(base + L.permP);
+    float *dinvP = (float *)(base + L.dinvP);
+    int *permS = (int *)(base + L.permS);
+    float *dinvS = (float *)(base + L.dinvS);
+    float *prow = (float *)(base + L.prow);
+    double *sc = (double *)(base + L.sc);
+    float2 *x32 = (float2 *)(base + L.x32);
+    float *P32 = (float *)(base + L.P32);
+    float *Pp = (float *)(base + L.Pp);
+    float *Sm = (float *)(base + L.Sm);
+    double *B = (double *)(base + L.B);
+    double *X = (double *)(base + L.X);
+    float *R32 = (float *)(base + L.R32);
+    float *U = (float *)(base + L.U);
+    float *Lam = (float *)(base + L.Lam);
+    float4 *bp = (float4 *)(base + L.bp);
+    const int r = ops.nops, p = ops.p, ldg = L.ldg, lds = L.lds;
+
+    bool need_rinv = false;
+    for (int q = 0; q < r; q++)
+        for (int c = 0; c < ops.op[q].ncomp; c++)
+            for (int t = 0; t < ops.op[q].c[c].nterm; t++) need_rinv |= ops.op[q].c[c].t[t].er < 0;
+
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t sys = gw; sys < a.nsys; sys += nw) {
+        const int j = a.sys_node[sys];
+        const int n = a.n_node ? a.n_node[j] : a.n;
+        const int deg = a.deg_node ? a.deg_node[j] : a.deg;
+        const int m = npoly(deg), s = n + m;
+        double2 xc;
+        double sx, sy;
+        load_stencil(a, j, n, xs, sid, xc, sx, sy, lane);
+        for (int l = lane; l < n; l += 32) {
+            const float2 v = make_float2(f64_to_f32(xs[2 * l]), f64_to_f32(xs[2 * l + 1]));
+            x32[l] = v;
+            monomial_row<float>(v.x, v.y, deg, P32 + l * m, 1);
+        }
+        if (lane < 2 * r) {
+            const int q = lane >> 1, c = lane & 1;
+            if (c < ops.op[q].ncomp) sc[lane] = ipow(sx, ops.op[q].c[c].a) * ipow(sy, ops.op[q].c[c].b);
+        }
+        __syncwarp();
+        RegRows<SP> RP;
+        fill_phi_rows<SP>(RP, x32, n, p, lane);
+        bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
+        if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
+        bool fallback = !ok;
+        if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, lane);
+        int64_t r0, r1;
+        system_rows(a, sys, j, r0, r1);
+        int iters_max = 0;
+        for (int64_t t = r0; t < r1 && !fallback; t++) {
+            const int64_t row = row_id(a, t);
+            const double2 yp = eval_point(a, row);
+            const double yx = (yp.x - xc.x) * sx, yy = (yp.y - xc.y) * sy;
+            build_rhs_schur(ops, xs, n, m, yx, yy, sc, need_rinv, B, lane);
+            float e_prev = 1.0f;
+            bool conv = false;
+            int it;
+            for (it = 0; it < a.max_refine; it++) {
+                if (it == 0) {
+                    for (int e = lane; e < s * r; e += 32) R32[e] = f64_to_f32(B[e]);
+                    __syncwarp();
+                } else {
+                    residual_schur<SP, RMAX>(phiP, P, n, m, r, B, X, R32, lane);
+                }
+                schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
+                unsigned dkey = 0u, xkey = 0u;
+                for (int e = lane; e < s * r; e += 32) {
+                    const float d = R32[e];
+                    const double xv = it == 0 ? f32_to_f64(d) : X[e] + f32_to_f64(d);
+                    X[e] = xv;
+                    if (e < n * r) {
+                        dkey = max(dkey, __float_as_uint(d) & 0x7fffffffu);
+                        xkey = max(xkey, (unsigned)__double2hiint(xv) & 0x7fffffffu);
+                    }
+                }
+                dkey = __reduce_max_sync(RBFFD_FULL, dkey);
+                xkey = __reduce_max_sync(RBFFD_FULL, xkey);
+                __syncwarp();
+                const float dmax = __uint_as_float(dkey);
+                const float xmax = f64_to_f32(__hiloint2double((int)xkey, 0));
+                const float e_cur = xmax > 0.0f ? __fdividef(dmax, xmax) : 0.0f;
+                if (!(e_cur == e_cur) || isinf(e_cur)) break;
+                if (it >= 1) {
+                    const float rho = e_prev > 0.0f ? __fdividef(e_cur, e_prev) : 0.0f;
+                    if ((double)rho * (double)e_cur <= a.refine_tol || e_cur == 0.0f) {
+                        conv = true;
+                        break;
+                    }
+                    if (rho > 0.5f) break;
+                }
+                e_prev = e_cur;
+            }
+            if (!conv) {
+                fallback = true;
+                break;
+            }
+            if (it > iters_max) iters_max = it;
+            write_row(a, ops, row, X, n, sid, sx, sy, lane);
+            __syncwarp();
+        }
+        if (lane == 0) {
+            if (fallback) {
+                const int pos = atomicAdd(a.fallback_count, 1);
+                a.fallback_list[pos] = (int32_t)sys;
+            } else {
+                atomicAdd(&a.hist[iters_max < 7 ? iters_max : 7], 1ull);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int SP, int SM, int RMAX>
+cudaError_t launch_schur(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st)
+{
+    const size_t per_warp = make_schur_layout(SP, SM, a.max_n, a.max_m, ops.nops).total;
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    while (wpb > 1 && per_warp * wpb > (size_t)smem_max) wpb--;
+    if (per_warp * wpb > (size_t)smem_max) return cudaErrorNotSupported;
+    const size_t smem = per_warp * wpb;
+    auto kern = solve_mixed_schur_kernel<SP, SM, RMAX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, wpb * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    const int64_t want = (a.nsys + wpb - 1) / wpb;
+    const int64_t cap = (int64_t)num_sms * occ;
+    const int blocks = (int)(want < cap ? want : cap);
+    kern<<<blocks, wpb * 32, smem, st>>>(a, ops);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Launchers of the Schur-complement kernel for stencils of at most 32 (weights_reg.cu) and at
+// most 64 nodes (weights_reg64.cu).  SM (16 or 32) bounds the number of monomials and RMAX
+// (4 or 8) the number of operators.
+cudaError_t launch_schur_sp32(const SolveArgs &a, const OpTable &ops, int SM, int RMAX, int wpb, int num_sms,
+                              cudaStream_t st);
+cudaError_t launch_schur_sp64(const SolveArgs &a, const OpTable &ops, int SM, int RMAX, int wpb, int num_sms,
+                              cudaStream_t st);
+size_t schur_smem_per_warp(int SP, int SM, int max_n, int max_m, int nops);
