@@ -436,7 +436,7 @@ def run_ours(args):
                       "grid": float(np.mean([s["ms_grid"] for s in st_mixed]))},
         "measured_fma_peaks_tflops": {"fp64": fp64_peak.value, "fp32": fp32_peak.value},
         "roofline": {
-            "kernel": "solve_mixed_kernel",
+            "kernel": "solve_mixed_schur_kernel",
             "bound": "fp64",
             "achieved": solve_ach,
             "peak": fp64_peak.value,

@@ -60,83 +60,6 @@ __device__ __forceinline__ float sel_f32(bool c, float a, float b)
     return r;
 }
 
-// float -> double from the IEEE-754 bit fields (exact for normal numbers; subnormals flush to
-// a signed zero; inf and NaN are kept).
-__device__ __forceinline__ double f32_to_f64(float f)
-{
-    unsigned u = __float_as_uint(f);
-    unsigned e = (u >> 23) & 0xffu;
-    unsigned sign = u & 0x80000000u;
-    unsigned mant = u & 0x7fffffu;
-    unsigned e64 = e == 255u ? 2047u : e + (1023u - 127u);
-    unsigned hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
-    unsigned lo = e == 0u ? 0u : (mant << 29);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
-// double -> float by truncation of the mantissa (|error| < 1 ulp of float), from the bit
-// fields.  Magnitudes above the float range give inf, below the normal range a signed zero;
-// NaN stays NaN.
-__device__ __forceinline__ float f64_to_f32(double d)
-{
-    unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    unsigned sign = hi & 0x80000000u;
-    int e = (int)((hi >> 20) & 0x7ffu);
-    int e32 = e - 1023 + 127;
-    unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    unsigned out;
-    if (e == 2047)
-        out = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
-    else if (e32 >= 255)
-        out = sign | 0x7f800000u;
-    else if (e32 <= 0)
-        out = sign;
-    else
-        out = sign | ((unsigned)e32 << 23) | mant;
-    return __uint_as_float(out);
-}
-
-// sqrt(a) for a positive normal double, without a library call: an FP32 reciprocal square
-// root of the mantissa (exponent split off on the integer pipe, a = a' 4^k with a' in [1, 4))
-// seeds Heron's iteration s <- s + (a - s^2) / (2 s), with 1 / (2 s) taken from the seed;
-// the error goes 2^-22 -> 2^-44 -> below FP64 rounding.  y0 returns the seed (~1/sqrt(a)).
-__device__ __forceinline__ double sqrt_nr(double a, double &y0)
-{
-    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
-    const int ex = (int)((hi >> 20) & 0x7ffu) - 1023;
-    const int k = ex >> 1;  // floor(ex / 2)
-    const unsigned fb = ((unsigned)(ex - 2 * k + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const float yf = rsqrtf(__uint_as_float(fb));
-    const double yd = f32_to_f64(yf);
-    y0 = __hiloint2double(__double2hiint(yd) - k * (1 << 20), __double2loint(yd));  // yf 2^-k
-    const double h = __hiloint2double(__double2hiint(y0) - (1 << 20), __double2loint(y0));  // y0 / 2
-    double s = a * y0;
-    s = fma(fma(-s, s, a), h, s);
-    return fma(fma(-s, s, a), h, s);
-}
-
-// 1/s from a seed y0 ~ 1/s (relative error ~2^-22) by two Newton-Raphson steps
-// y <- y + y (1 - s y).
-__device__ __forceinline__ double recip_nr(double s, double y0)
-{
-    double y = fma(y0, fma(-s, y0, 1.0), y0);
-    return fma(y, fma(-s, y, 1.0), y);
-}
-
-// phi = r^p from r^2 without library calls (r^2 = 0 gives 0).
-__device__ __forceinline__ double phi64_nr(double r2, int p)
-{
-    double v = r2;
-    for (int i = 1; i < (p >> 1); i++) v *= r2;
-    if (p < 2) v = 1.0;
-    if (p & 1) {
-        double y0;
-        const double rt = sqrt_nr(r2, y0);
-        v *= rt;
-    }
-    return r2 > 0.0 ? v : 0.0;
-}
-
 template <int S>
 struct RegRows {
     static constexpr int NS = (S + 31) / 32;
@@ -521,75 +444,74 @@ __device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int 
 // i (i + 1) / 2 + j.
 __device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
 
-// R32 <- float(B - A X) with FP64 products: Phi rows lane-per-row (all operators of a row per
-// lane, so each Phi element is loaded once), P' rows lane-per-element.
-template <int SP, int RMAX>
+// NE (1 or 2) elements (i, q) of r = b - A x for the Phi rows, elements e0 + lane + 32 u.
+template <int NE>
+__device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r,
+                                                  const double *B, const double *X, float *R32, int e0, int lane)
+{
+    const int tot = n * r;
+    int ee[NE], ii[NE], qq[NE], off[NE];
+    double a0[NE], a1[NE];
+#pragma unroll
+    for (int u = 0; u < NE; u++) {
+        ee[u] = e0 + lane + 32 * u;
+        const int ec = ee[u] < tot ? ee[u] : tot - 1;
+        ii[u] = ec / r;
+        qq[u] = ec - ii[u] * r;
+        off[u] = tri_off(ii[u]);
+        a0[u] = B[ec];
+        a1[u] = 0.0;
+    }
+    int offj = 0;  // tri_off(jj)
+    int jj = 0;
+    for (; jj + 2 <= n; jj += 2) {
+        const int offj1 = offj + jj + 1;
+#pragma unroll
+        for (int u = 0; u < NE; u++) {
+            const int ad0 = jj <= ii[u] ? off[u] + jj : offj + ii[u];
+            const int ad1 = jj + 1 <= ii[u] ? off[u] + jj + 1 : offj1 + ii[u];
+            a0[u] = fma(-phiP[ad0], X[jj * r + qq[u]], a0[u]);
+            a1[u] = fma(-phiP[ad1], X[(jj + 1) * r + qq[u]], a1[u]);
+        }
+        offj = offj1 + jj + 2;
+    }
+    if (jj < n) {
+#pragma unroll
+        for (int u = 0; u < NE; u++) {
+            const int ad0 = jj <= ii[u] ? off[u] + jj : offj + ii[u];
+            a0[u] = fma(-phiP[ad0], X[jj * r + qq[u]], a0[u]);
+        }
+    }
+    const double *Xl = X + n * r;
+    int l = 0;
+    for (; l + 2 <= m; l += 2) {
+#pragma unroll
+        for (int u = 0; u < NE; u++) {
+            a0[u] = fma(-P[ii[u] * m + l], Xl[l * r + qq[u]], a0[u]);
+            a1[u] = fma(-P[ii[u] * m + l + 1], Xl[(l + 1) * r + qq[u]], a1[u]);
+        }
+    }
+    if (l < m) {
+#pragma unroll
+        for (int u = 0; u < NE; u++) a0[u] = fma(-P[ii[u] * m + l], Xl[l * r + qq[u]], a0[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < NE; u++)
+        if (ee[u] < tot) R32[ee[u]] = f64_to_f32(a0[u] + a1[u]);
+}
+
+// R32 <- float(B - A X) with FP64 products, lane-per-element: ceil(n r / 32) lane-full passes
+// of n + m FMAs for the Phi rows (two passes interleaved per lane), one pass of n FMAs per 32
+// elements for the P' rows.  Phi is read from its packed lower triangle.
 __device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r,
                                               const double *B, const double *X, float *R32, int lane)
 {
-    constexpr int NS = SP / 32;
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-        if (32 * k >= n) break;
-        const int i = lane + 32 * k;
-        const bool act = i < n;
-        const int ii = act ? i : n - 1;
-        double a0[RMAX], a1[RMAX];
-#pragma unroll
-        for (int q = 0; q < RMAX; q++) {
-            a0[q] = 0.0;
-            a1[q] = 0.0;
-            if (q < r) a0[q] = B[ii * r + q];
-        }
-        const int offi = tri_off(ii);
-        int offj = 0;  // tri_off(jj)
-        int jj = 0;
-        for (; jj + 2 <= n; jj += 2) {
-            const int ad0 = jj <= ii ? offi + jj : offj + ii;
-            offj += jj + 1;
-            const int ad1 = jj + 1 <= ii ? offi + jj + 1 : offj + ii;
-            offj += jj + 2;
-            const double f0 = phiP[ad0], f1 = phiP[ad1];
-            const double *x0 = X + jj * r;
-#pragma unroll
-            for (int q = 0; q < RMAX; q++) {
-                if (q < r) {
-                    a0[q] = fma(-f0, x0[q], a0[q]);
-                    a1[q] = fma(-f1, x0[r + q], a1[q]);
-                }
-            }
-        }
-        if (jj < n) {
-            const int ad0 = jj <= ii ? offi + jj : offj + ii;
-            const double f0 = phiP[ad0];
-#pragma unroll
-            for (int q = 0; q < RMAX; q++)
-                if (q < r) a0[q] = fma(-f0, X[jj * r + q], a0[q]);
-        }
-        const double *Pi = P + ii * m;
-        const double *Xl = X + n * r;
-        int l = 0;
-        for (; l + 2 <= m; l += 2) {
-            const double p0 = Pi[l], p1 = Pi[l + 1];
-#pragma unroll
-            for (int q = 0; q < RMAX; q++) {
-                if (q < r) {
-                    a0[q] = fma(-p0, Xl[l * r + q], a0[q]);
-                    a1[q] = fma(-p1, Xl[(l + 1) * r + q], a1[q]);
-                }
-            }
-        }
-        if (l < m) {
-            const double p0 = Pi[l];
-#pragma unroll
-            for (int q = 0; q < RMAX; q++)
-                if (q < r) a0[q] = fma(-p0, Xl[l * r + q], a0[q]);
-        }
-        if (act) {
-#pragma unroll
-            for (int q = 0; q < RMAX; q++)
-                if (q < r) R32[i * r + q] = f64_to_f32(a0[q] + a1[q]);
-        }
+    const int tot = n * r;
+    for (int e0 = 0; e0 < tot; e0 += 64) {
+        if (e0 + 32 < tot)
+            residual_phi_rows<2>(phiP, P, n, m, r, B, X, R32, e0, lane);
+        else
+            residual_phi_rows<1>(phiP, P, n, m, r, B, X, R32, e0, lane);
     }
     for (int e = lane; e < m * r; e += 32) {
         const int l = e / r, q = e - l * r;
@@ -644,8 +566,9 @@ __device__ __forceinline__ int ifact(int e)
 }
 
 // Right-hand sides of one evaluation point y~ (scaled coordinates) into B (s x r).  Same
-// formulas as build_rhs, with r and 1/r from sqrt_nr / recip_nr, per-system scale factors sc[2 q + c] = sx^a sy^b precomputed, and the polynomial rows
-// of a point at the stencil centre (y~ = 0: the common collocated case) from integers.
+// formulas as build_rhs, with r and 1/r from sqrt_nr / recip_nr, per-system scale factors
+// sc[2 q + c] = sx^a sy^b precomputed, and the polynomial rows of a point at the stencil
+// centre (y~ = 0: the common collocated case) from integers.
 __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double *xs, int n, int m, double yx,
                                                 double yy, const double *sc, bool need_rinv, double *B, int lane)
 {
@@ -742,6 +665,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
     float4 *bp = (float4 *)(base + L.bp);
     const int r = ops.nops, p = ops.p, ldg = L.ldg, lds = L.lds;
 
+    const float tol32 = f64_to_f32(a.refine_tol);
     bool need_rinv = false;
     for (int q = 0; q < r; q++)
         for (int c = 0; c < ops.op[q].ncomp; c++)
@@ -789,7 +713,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                     for (int e = lane; e < s * r; e += 32) R32[e] = f64_to_f32(B[e]);
                     __syncwarp();
                 } else {
-                    residual_schur<SP, RMAX>(phiP, P, n, m, r, B, X, R32, lane);
+                    residual_schur(phiP, P, n, m, r, B, X, R32, lane);
                 }
                 schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
                 unsigned dkey = 0u, xkey = 0u;
@@ -811,7 +735,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                 if (!(e_cur == e_cur) || isinf(e_cur)) break;
                 if (it >= 1) {
                     const float rho = e_prev > 0.0f ? __fdividef(e_cur, e_prev) : 0.0f;
-                    if ((double)rho * (double)e_cur <= a.refine_tol || e_cur == 0.0f) {
+                    if (rho * e_cur <= tol32 || e_cur == 0.0f) {
                         conv = true;
                         break;
                     }

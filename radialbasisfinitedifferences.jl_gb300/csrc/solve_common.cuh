@@ -91,6 +91,83 @@ __device__ __forceinline__ float warp_max_f(float v)
 
 __device__ __forceinline__ bool is_zero64(double x) { return abs_key(x) == 0ull; }
 
+// float -> double from the IEEE-754 bit fields (exact for normal numbers; subnormals flush to
+// a signed zero; inf and NaN are kept).
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    unsigned u = __float_as_uint(f);
+    unsigned e = (u >> 23) & 0xffu;
+    unsigned sign = u & 0x80000000u;
+    unsigned mant = u & 0x7fffffu;
+    unsigned e64 = e == 255u ? 2047u : e + (1023u - 127u);
+    unsigned hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
+    unsigned lo = e == 0u ? 0u : (mant << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float by truncation of the mantissa (|error| < 1 ulp of float), from the bit
+// fields.  Magnitudes above the float range give inf, below the normal range a signed zero;
+// NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32(double d)
+{
+    unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    unsigned sign = hi & 0x80000000u;
+    int e = (int)((hi >> 20) & 0x7ffu);
+    int e32 = e - 1023 + 127;
+    unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned out;
+    if (e == 2047)
+        out = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
+    else if (e32 >= 255)
+        out = sign | 0x7f800000u;
+    else if (e32 <= 0)
+        out = sign;
+    else
+        out = sign | ((unsigned)e32 << 23) | mant;
+    return __uint_as_float(out);
+}
+
+// sqrt(a) for a positive normal double, without a library call: an FP32 reciprocal square
+// root of the mantissa (exponent split off on the integer pipe, a = a' 4^k with a' in [1, 4))
+// seeds Heron's iteration s <- s + (a - s^2) / (2 s), with 1 / (2 s) taken from the seed;
+// the error goes 2^-22 -> 2^-44 -> below FP64 rounding.  y0 returns the seed (~1/sqrt(a)).
+__device__ __forceinline__ double sqrt_nr(double a, double &y0)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const int ex = (int)((hi >> 20) & 0x7ffu) - 1023;
+    const int k = ex >> 1;  // floor(ex / 2)
+    const unsigned fb = ((unsigned)(ex - 2 * k + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const float yf = rsqrtf(__uint_as_float(fb));
+    const double yd = f32_to_f64(yf);
+    y0 = __hiloint2double(__double2hiint(yd) - k * (1 << 20), __double2loint(yd));  // yf 2^-k
+    const double h = __hiloint2double(__double2hiint(y0) - (1 << 20), __double2loint(y0));  // y0 / 2
+    double s = a * y0;
+    s = fma(fma(-s, s, a), h, s);
+    return fma(fma(-s, s, a), h, s);
+}
+
+// 1/s from a seed y0 ~ 1/s (relative error ~2^-22) by two Newton-Raphson steps
+// y <- y + y (1 - s y).
+__device__ __forceinline__ double recip_nr(double s, double y0)
+{
+    double y = fma(y0, fma(-s, y0, 1.0), y0);
+    return fma(y, fma(-s, y, 1.0), y);
+}
+
+// phi = r^p from r^2 without library calls.
+__device__ __forceinline__ double phi64_nr(double r2, int p)
+{
+    double v = r2;
+    for (int i = 1; i < (p >> 1); i++) v *= r2;
+    if (p < 2) v = 1.0;
+    if (p & 1) {
+        double y0;
+        const double rt = sqrt_nr(r2, y0);
+        v *= rt;
+    }
+    return r2 >= DBL_MIN ? v : 0.0;  // r^p of a subnormal r^2 underflows to 0 in FP64
+}
+
 // phi = r^p from r^2 (odd p: r^(p-1) * r; even p: (r^2)^(p/2)).
 __device__ __forceinline__ double phi64(double r2, int p)
 {
@@ -443,7 +520,7 @@ __device__ __forceinline__ void assemble64(double *A, int lda, const double *xs,
         int i, j;
         tri_pair(t, n, i, j);
         double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
-        double v = phi64(fma(dx, dx, dy * dy), p);
+        double v = phi64_nr(fma(dx, dx, dy * dy), p);
         A[i * lda + j] = v;
         A[j * lda + i] = v;
     }
@@ -514,8 +591,16 @@ __device__ __forceinline__ void build_rhs(const OpTable &ops, const double *xs, 
             if (is_zero64(cx)) cx = EPS64;
             if (is_zero64(cy)) cy = EPS64;
         }
-        double rr = sqrt(fma(cx, cx, cy * cy));
-        double rinv = 1.0 / rr;
+        const double r2 = fma(cx, cx, cy * cy);
+        double rr, rinv;
+        if (r2 >= DBL_MIN && r2 <= 1e300) {
+            double y0;
+            rr = sqrt_nr(r2, y0);
+            rinv = recip_nr(rr, y0);
+        } else {
+            rr = sqrt(r2);
+            rinv = 1.0 / rr;
+        }
         int row = pinv ? pinv[i] : i;
         for (int q = 0; q < r; q++) {
             const OpDesc &od = ops.op[q];
