@@ -41,6 +41,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--workload", default="collocated", choices=["collocated", "uneven", "rk4"],
+                    help="collocated: the headline line; uneven: mixed stencil sizes with boundary and ghost "
+                         "classes (2,097,152 nodes); rk4: advection-diffusion-hyperviscosity RK4 on 2048^2 nodes")
+    ap.add_argument("--total", type=int, default=2_097_152, help="uneven: number of nodes")
+    ap.add_argument("--rk-nx", type=int, default=2048, help="rk4: grid side")
+    ap.add_argument("--rk-steps", type=int, default=100, help="rk4: time steps per precision")
+    ap.add_argument("--rk-fields", type=int, default=64, help="rk4: fields advanced together")
     return ap.parse_args()
 
 
@@ -331,7 +338,8 @@ def run_ours(args):
             spmv_times.append(e0.elapsed_time(e1))
     spmv_ms = float(np.mean(spmv_times))
     nnz = s.nnz
-    spmv_bytes = nnz * (8 + 4) + (rows_per + 1) * 8 + N * 8 + rows_per * 8
+    # algorithmic bytes: weights + int32 columns, row pointers (int32 count), x read once, y written once
+    spmv_bytes = nnz * (8 + 4) + (rows_per + 1) * 4 + N * 8 + rows_per * 8
     spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
     s.close()
 
@@ -447,7 +455,7 @@ def run_ours(args):
                     "event-timed duration, against the measured FP64 FMA peak (rbffd_measure_fma_peaks)",
         },
         "roofline_apply": {
-            "kernel": "spmv_f64_kernel",
+            "kernel": "spmv_f64_pipe",
             "bound": "hbm",
             "achieved": spmv_gbs,
             "peak": hbm,
@@ -464,8 +472,166 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_uneven(args):
+    """Mixed stencil sizes, boundary and ghost classes: rectangle [0,2]x[0,1] with 4 boundaries
+    and one ghost layer, per-node (k, deg) in {(20,2), (30,3), (45,4), (60,5)} (85% (30,3)),
+    boundary-class-masked kNN, Dx/Dy/Lap with PHS r^3 and Dxk/Dyk (K=4) with PHS r^5; mixed
+    against plain FP64."""
+    import torch
+
+    import __graft_entry__
+
+    pkg = __graft_entry__.load_package()
+    d = pkg.nodesets.rectangle_with_ghosts(total=args.total, seed=4)
+    X, cls, nn, dd = d["X"], d["node_class"], d["n"], d["deg"]
+    h = pkg.Handle()
+    Xd = torch.tensor(X, device="cuda")
+    cd = torch.tensor(cls, dtype=torch.int32, device="cuda")
+    nd = torch.tensor(nn, dtype=torch.int32, device="cuda")
+    ddev = torch.tensor(dd, dtype=torch.int32, device="cuda")
+    sets = {"ops": (3, ("Dx", "Dy", "Lap"), 0), "hyperviscosity": (5, ("Dxk", "Dyk"), 4)}
+    res = {}
+    vals = {}
+    for name, (p, ops, kd) in sets.items():
+        for prec in ("mixed", "fp64"):
+            ts, st = [], None
+            for it in range(args.warmup + args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                s = pkg.OperatorSet(Xd, None, p, 0, 0, ops=ops, precision=prec, node_class=cd, n_per_node=nd,
+                                    deg_per_node=ddev, k_deriv=kd, handle=h, device=True)
+                torch.cuda.synchronize()
+                if it >= args.warmup:
+                    ts.append(time.perf_counter() - t0)
+                st = s.stats.as_dict()
+                if it == args.warmup + args.steps - 1:
+                    rp = s.device_csr(ops[0])[0]
+                    rpt = torch.as_tensor(pkg.operators._DeviceArray(rp, s.rows + 1, "<i8"), device="cuda").clone()
+                    vals[(name, prec)] = ([s.device_values(o).clone() for o in ops], rpt)
+                s.close()
+            ms = 1e3 * float(np.mean(ts))
+            res[f"{name}_{prec}"] = {"solves_per_s": len(X) / (ms * 1e-3), "ms_per_build": ms,
+                                     "ms_knn": st["ms_knn"], "ms_solve": st["ms_solve"],
+                                     "ms_fallback": st["ms_fallback"], "fallback": st["n_fallback"],
+                                     "refine_hist": st["refine_hist"], "kernel_launches": st["kernel_launches"]}
+        errs = {}
+        rpt = vals[(name, "fp64")][1]
+        lengths = rpt[1:] - rpt[:-1]
+        rid = torch.repeat_interleave(torch.arange(len(lengths), device="cuda"), lengths)
+        for q, o in enumerate(sets[name][1]):
+            a, b = vals[(name, "mixed")][0][q], vals[(name, "fp64")][0][q]
+            num = torch.zeros(len(lengths), dtype=torch.float64, device="cuda").scatter_reduce_(
+                0, rid, (a - b).abs(), "amax")
+            den = torch.zeros_like(num).scatter_reduce_(0, rid, b.abs(), "amax")
+            e = num / den
+            errs[o] = {"max": float(e.max().item()), "median": float(e.median().item())}
+        res[f"{name}_row_rel_err_mixed_vs_fp64"] = errs
+        res[f"{name}_mixed_over_fp64"] = res[f"{name}_fp64"]["ms_solve"] / res[f"{name}_mixed"]["ms_solve"]
+    out = {"workload": "uneven: rectangle [0,2]x[0,1], 4 boundaries + ghosts, per-node (k,deg) "
+                       "{(20,2),(30,3),(45,4),(60,5)}, boundary-masked kNN",
+           "nodes": int(len(X)), "counts": d["counts"],
+           "steps": args.steps, "warmup": args.warmup, "timing": "wall clock of the whole device build, "
+           "inputs resident in HBM", **res}
+    print(json.dumps(out))
+
+
+def run_rk4(args):
+    """du/dt = L u, L = -a.grad + nu Lap - gamma (Dxk + Dyk), a = (1, 0.5), nu = 1e-3,
+    gamma = 100 h^4 (examples/adv_diff_test.jl:152), Dxk/Dyk with K = 4 and PHS r^5; RK4 with
+    dt = 0.2 h (reduced to the largest stable step when rho(L) dt exceeds RK4's real-axis
+    limit), rows within one spacing of the boundary held fixed, F fields of 8 seeded Gaussians;
+    FP64 and FP32 weights and fields, drift ||u32 - u64|| / ||u64||."""
+    import torch
+
+    import __graft_entry__
+
+    pkg = __graft_entry__.load_package()
+    nx = args.rk_nx
+    X, hh, _ = pkg.nodesets.jittered_grid(nx, seed=5)
+    N = len(X)
+    h = pkg.Handle()
+    Xd = torch.tensor(X, device="cuda")
+    t0 = time.perf_counter()
+    s3 = pkg.OperatorSet(Xd, None, 3, 30, 3, ops=("Dx", "Dy", "Lap"), precision="mixed", handle=h, device=True)
+    s5 = pkg.OperatorSet(Xd, None, 5, 30, 3, ops=("Dxk", "Dyk"), precision="mixed", k_deriv=4, handle=h,
+                         device=True)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    nu, gamma = 1e-3, 100.0 * hh ** 4
+    coef = [-1.0, -0.5, nu, -gamma, -gamma]
+    fixed = ((X[:, 0] < hh) | (X[:, 0] > 1 - hh) | (X[:, 1] < hh) | (X[:, 1] > 1 - hh)).astype(np.uint8)
+    F = args.rk_fields
+    rng = np.random.default_rng(11)
+    cx, cy = rng.uniform(0, 1, (F, 8)), rng.uniform(0, 1, (F, 8))
+    sg, am = rng.uniform(0.05, 0.15, (F, 8)), rng.uniform(-1, 1, (F, 8))
+    Xt = torch.tensor(X, device="cuda")
+    u0 = torch.zeros(N, F, dtype=torch.float64, device="cuda")
+    for f in range(F):
+        for g in range(8):
+            r2 = (Xt[:, 0] - cx[f, g]) ** 2 + (Xt[:, 1] - cy[f, g]) ** 2
+            u0[:, f] += am[f, g] * torch.exp(-r2 / (2 * sg[f, g] ** 2))
+    out = {"workload": f"rk4: {nx}x{nx} jittered nodes, k=30, deg 3, L = -a.grad + nu Lap - gamma (Dxk + Dyk)",
+           "nodes": N, "fields": F, "nnz_per_operator": s3.nnz, "build_s": t_build,
+           "fixed_rows": int(fixed.sum())}
+    rk = {}
+    for dt_name in ("f64", "f32"):
+        rk[dt_name] = pkg.RK4Stepper([s3, s5], coef, F, dtype=dt_name, fixed_rows=fixed, handle=h)
+    # rho(L) by power iteration on one field (FP64)
+    one = pkg.RK4Stepper([s3, s5], coef, 1, dtype="f64", fixed_rows=fixed, handle=h)
+    v = torch.randn(N, 1, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    v[torch.tensor(fixed, device="cuda").bool()] = 0
+    w = torch.empty_like(v)
+    lam = 0.0
+    for _ in range(60):
+        v /= v.norm()
+        one.apply(v, w)
+        lam = float(w.norm().item())
+        v, w = w, v
+    one.close()
+    dt = 0.2 * hh
+    limit = 2.78
+    stable = lam * dt <= limit
+    dt_used = dt if stable else 0.9 * limit / lam
+    out.update({"rho_L": lam, "dt_nominal": dt, "rho_dt_nominal": lam * dt, "rk4_limit": limit,
+                "stable_at_nominal_dt": bool(stable), "dt_used": dt_used})
+    res = {}
+    for dt_name, tdt in (("f64", torch.float64), ("f32", torch.float32)):
+        u = u0.to(tdt).contiguous()
+        rk[dt_name].run(u, dt_used, 2)  # warm-up (graph capture)
+        u = u0.to(tdt).contiguous()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_w = time.perf_counter()
+        e0.record()
+        rk[dt_name].run(u, dt_used, args.rk_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t_w) * 1e3
+        res[dt_name] = (u, ms)
+        sz = 8 if dt_name == "f64" else 4
+        nnz = s3.nnz
+        stage_bytes = nnz * (sz + 4) + 2 * N * F * sz
+        out[f"{dt_name}"] = {"ms_per_step": ms / args.rk_steps, "steps": args.rk_steps,
+                             "stage_algorithmic_GBps": 4 * args.rk_steps * stage_bytes / (ms * 1e-3) / 1e9,
+                             "stage_fma_TFLOPs": 4 * args.rk_steps * 2.0 * nnz * F / (ms * 1e-3) / 1e12,
+                             "finite": bool(torch.isfinite(u).all().item())}
+    u64, u32 = res["f64"][0], res["f32"][0].double()
+    out["drift_f32_vs_f64"] = float(((u32 - u64).norm() / u64.norm()).item())
+    for r in rk.values():
+        r.close()
+    s3.close()
+    s5.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.workload == "uneven":
+        run_uneven(args)
+        return
+    if args.workload == "rk4":
+        run_rk4(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

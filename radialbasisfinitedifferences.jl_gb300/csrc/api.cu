@@ -105,6 +105,50 @@ __global__ void uniform_ptr(int64_t *a, int64_t n, int64_t step)
         a[i] = i * step;
 }
 
+// Shape classes of the mixed solve kernels: bin = 2 * (n > 32) + (m > 16) for n <= 64 and
+// m <= 32 (the register kernels' instantiations), NBIN - 1 for anything larger.
+constexpr int NBIN = 5;
+__host__ __device__ inline int solve_bin(int n, int m)
+{
+    if (n > 64 || m > 32) return NBIN - 1;
+    return 2 * (n > 32 ? 1 : 0) + (m > 16 ? 1 : 0);
+}
+
+// Per-bin system counts and largest n, m (cnt[0..NBIN), maxn[NBIN..2NBIN), maxm[2NBIN..3NBIN)).
+__global__ void bin_count(const int32_t *sys_node, int64_t nsys, const int32_t *n_node, const int32_t *deg_node,
+                          int n0, int deg0, unsigned long long *cnt)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nsys;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int j = sys_node[t];
+        const int n = n_node ? n_node[j] : n0;
+        const int d = deg_node ? deg_node[j] : deg0;
+        const int m = (d + 1) * (d + 2) / 2;
+        const int b = solve_bin(n, m);
+        atomicAdd(cnt + b, 1ull);
+        atomicMax(cnt + NBIN + b, (unsigned long long)n);
+        atomicMax(cnt + 2 * NBIN + b, (unsigned long long)m);
+    }
+}
+
+struct BinOffsets {
+    int64_t off[NBIN];
+};
+
+__global__ void bin_scatter(const int32_t *sys_node, int64_t nsys, const int32_t *n_node, const int32_t *deg_node,
+                            int n0, int deg0, BinOffsets bo, unsigned long long *fill, int32_t *list)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nsys;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int j = sys_node[t];
+        const int n = n_node ? n_node[j] : n0;
+        const int d = deg_node ? deg_node[j] : deg0;
+        const int b = solve_bin(n, (d + 1) * (d + 2) / 2);
+        const unsigned long long pos = atomicAdd(fill + b, 1ull);
+        list[bo.off[b] + (int64_t)pos] = (int32_t)t;
+    }
+}
+
 __global__ void mark_nodes(const int32_t *nn, int64_t rows, int64_t *flag)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
@@ -650,6 +694,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     CK(keep.get(&val, (size_t)nnz * nops));
     // ---- weight solves
     SolveArgs a{};
+    int64_t n_bin_launches = 0, n_solve_launches = 1;
     a.X = dX;
     a.Y = collocated ? nullptr : dY;
     a.nbr = nbr;
@@ -680,13 +725,49 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         a.fallback_list = fb_list;
         a.fallback_count = &dflags->fallback_count;
         a.hist = dflags->hist;
-        cudaError_t e = launch_solve_mixed_reg(a, table, a.max_m, 4, h->num_sms, st);
-        if (e == cudaErrorNotSupported) {
-            cudaGetLastError();
-            int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(max_s, max_n, nops));
-            e = launch_solve_mixed(a, table, wpb, h->num_sms, st);
+        // one launch per shape class (per-node n / degree arrays), so that the many small
+        // stencils do not run with the shared-memory and register budget of the largest
+        std::vector<SolveArgs> launches;
+        if ((dn || ddeg) && nsys > 0) {
+            unsigned long long *cnt, hc[3 * NBIN];
+            int32_t *list;
+            CK(tmp.zeros(&cnt, 4 * NBIN));
+            CK(tmp.get(&list, nsys));
+            bin_count<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, cnt);
+            CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            BinOffsets bo;
+            int64_t o = 0;
+            for (int b = 0; b < NBIN; b++) {
+                bo.off[b] = o;
+                o += (int64_t)hc[b];
+            }
+            bin_scatter<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, bo,
+                                                    cnt + 3 * NBIN, list);
+            n_bin_launches = 2;
+            for (int b = 0; b < NBIN; b++) {
+                if (hc[b] == 0) continue;
+                SolveArgs ab = a;
+                ab.sys_list = list + bo.off[b];
+                ab.nsys = (int64_t)hc[b];
+                ab.max_n = (int)hc[NBIN + b];
+                ab.max_m = (int)hc[2 * NBIN + b];
+                ab.max_s = ab.max_n + ab.max_m;
+                launches.push_back(ab);
+            }
+        } else {
+            launches.push_back(a);
         }
-        CK(e);
+        for (const SolveArgs &ab : launches) {
+            cudaError_t e = launch_solve_mixed_reg(ab, table, ab.max_m, 4, h->num_sms, st);
+            if (e == cudaErrorNotSupported) {
+                cudaGetLastError();
+                int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(ab.max_s, ab.max_n, nops));
+                e = launch_solve_mixed(ab, table, wpb, h->num_sms, st);
+            }
+            CK(e);
+        }
+        n_solve_launches = (int64_t)launches.size();
     } else {
         int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
         CK(launch_solve_fp64(a, table, wpb, h->num_sms, st));
@@ -728,7 +809,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         if (!uniform) nk += (dn ? 1 : 0) + 3;
         nk += 1;
         nk += uniform ? 1 : 4;
-        nk += 1;
+        nk += n_bin_launches + n_solve_launches;
         if (pb->precision == RBFFD_PREC_MIXED && hf.fallback_count > 0) nk += 1;
         stats->kernel_launches = nk;
     }

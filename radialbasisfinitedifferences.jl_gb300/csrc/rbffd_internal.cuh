@@ -114,7 +114,8 @@ struct SolveArgs {
     const int32_t *n_node;     // nullable per-node stencil size
     const int32_t *deg_node;   // nullable per-node degree
     int n, deg;                // uniform values
-    const int32_t *sys_node;   // nsys X nodes to factor
+    const int32_t *sys_node;   // X node of every system
+    const int32_t *sys_list;   // nullable: this launch solves systems sys_list[0..nsys), else 0..nsys
     const int64_t *sys_rows;   // nullable: rows of system i are rows_list[sys_rows[i]..sys_rows[i+1])
     const int32_t *rows_list;  // row ids (global evaluation-point ids)
     int64_t nsys;

@@ -154,6 +154,22 @@ __device__ __forceinline__ double recip_nr(double s, double y0)
     return fma(y, fma(-s, y, 1.0), y);
 }
 
+// 1/a for a finite nonzero double: FP32 reciprocal of the mantissa (the exponent split off on
+// the integer pipe) refined by two Newton-Raphson steps y <- y + y (1 - a y), error
+// 2^-22 -> 2^-44 -> rounding level; subnormal a takes the division.
+__device__ __forceinline__ double recip64(double a)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const int ex = (int)((hi >> 20) & 0x7ffu) - 1023;
+    if (ex == -1023) return 1.0 / a;
+    const unsigned fb = (hi & 0x80000000u) | (127u << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const float yf = __fdividef(1.0f, __uint_as_float(fb));  // mantissa in [1, 2): |yf| in (0.5, 1]
+    const double yd = f32_to_f64(yf);
+    double y = __hiloint2double(__double2hiint(yd) - ex * (1 << 20), __double2loint(yd));
+    y = fma(y, fma(-a, y, 1.0), y);
+    return fma(y, fma(-a, y, 1.0), y);
+}
+
 // phi = r^p from r^2 without library calls.
 __device__ __forceinline__ double phi64_nr(double r2, int p)
 {
@@ -264,7 +280,7 @@ __device__ bool warp_lu64(double *A, int lda, int s, int *piv, double *dinv, int
                 A[bi * lda + j] = t;
             }
         __syncwarp();
-        double rinv = 1.0 / A[c * lda + c];
+        double rinv = recip64(A[c * lda + c]);
         if (lane == 0) dinv[c] = rinv;
         for (int i = c + 1 + lane; i < s; i += 32) A[i * lda + c] *= rinv;
         __syncwarp();
@@ -501,8 +517,8 @@ __device__ __forceinline__ void load_stencil(const SolveArgs &a, int j, int n, d
     } else {
         mx = warp_max_abs(mx);
         my = warp_max_abs(my);
-        sx = 1.0 / mx;
-        sy = 1.0 / my;
+        sx = recip64(mx);  // 1.0 / max|x_j - x_c| (src/scalestencil.jl:17-18)
+        sy = recip64(my);
         for (int l = lane; l < n; l += 32) {
             xs[2 * l] *= sx;
             xs[2 * l + 1] *= sy;

@@ -64,52 +64,84 @@ __global__ void __launch_bounds__(256) spmv_f64_uniform(int64_t rows, const int3
     }
 }
 
-// Uniform stencil size K (even), staged: each warp owns tiles of 32 consecutive rows, whose
-// weights (32*K doubles) and column ids (32*K ints) are contiguous in HBM.  The warp copies
-// a tile into its shared-memory slot with fully coalesced 16-byte loads (4 L1 wavefronts per
-// instruction instead of 32 for per-thread row loads), then each lane accumulates its own
-// row from shared memory (row stride K*8 bytes = odd multiple of 16 for K = 2 mod 4:
-// conflict-free LDS.128) with x gathered through L1/L2.
+// 16-byte asynchronous global -> shared copy that skips L1 and marks the line evict-first in
+// L2 (the streamed weights and column ids must not push the gathered x out of L2).
+__device__ __forceinline__ void cp_async16_stream(void *smem, const void *gmem, unsigned long long pol)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Uniform stencil size K (even), two-stage pipeline: each warp owns tiles of 32 consecutive
+// rows (weights 32*K doubles and column ids 32*K ints, contiguous and 16-byte aligned in HBM)
+// and copies the next tile into its second shared-memory stage with cp.async while it
+// computes the current one, so HBM streaming overlaps the FP64 FMAs (31.5M FMAs take ~50 us
+// at GB300's FP64 rate, about as long as streaming their 378 MB).  Each lane accumulates its
+// own row from shared memory in two independent chains; x is gathered through L1/L2.
 template <int K>
-__global__ void __launch_bounds__(256) spmv_f64_staged(int64_t rows, const int32_t *__restrict__ col,
-                                                       const double *__restrict__ val,
-                                                       const double *__restrict__ x, double *__restrict__ y)
+__global__ void __launch_bounds__(256) spmv_f64_pipe(int64_t rows, const int32_t *__restrict__ col,
+                                                     const double *__restrict__ val,
+                                                     const double *__restrict__ x, double *__restrict__ y)
 {
     static_assert(K % 2 == 0, "even K");
-    constexpr int VB = 32 * K * 8, CB = 32 * K * 4;
+    constexpr int VB = 32 * K * 8, CB = 32 * K * 4, STB = VB + CB;
     extern __shared__ __align__(16) unsigned char sm_dyn[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned char *mine = sm_dyn + (size_t)w * (VB + CB);
-    double *sv = reinterpret_cast<double *>(mine);
-    int *sc = reinterpret_cast<int *>(mine + VB);
-    int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    unsigned char *mine = sm_dyn + (size_t)w * 2 * STB;
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
     const int64_t ntile = (rows + 31) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (; tile < ntile; tile += nw) {
+    const int64_t first = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+
+    auto issue = [&](int64_t tile, int stage) {
         const int64_t r0 = tile * 32;
         const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
-        const int nv2 = nr * K / 2;  // double2 chunks
+        double *sv = reinterpret_cast<double *>(mine + stage * STB);
+        int *sc = reinterpret_cast<int *>(mine + stage * STB + VB);
         const double2 *gv = reinterpret_cast<const double2 *>(val + r0 * K);
-        for (int c = lane; c < nv2; c += 32) reinterpret_cast<double2 *>(sv)[c] = __ldcs(gv + c);
+        const int nv2 = nr * K / 2;
+        for (int c = lane; c < nv2; c += 32) cp_async16_stream(reinterpret_cast<double2 *>(sv) + c, gv + c, pol);
         const int nc = nr * K, nc4 = nc >> 2;
         const int4 *gc = reinterpret_cast<const int4 *>(col + r0 * K);
-        for (int c = lane; c < nc4; c += 32) reinterpret_cast<int4 *>(sc)[c] = __ldcs(gc + c);
+        for (int c = lane; c < nc4; c += 32) cp_async16_stream(reinterpret_cast<int4 *>(sc) + c, gc + c, pol);
         for (int c = 4 * nc4 + lane; c < nc; c += 32) sc[c] = __ldcs(col + r0 * K + c);
+    };
+
+    if (first < ntile) issue(first, 0);
+    cp_async_commit();
+    int stage = 0;
+    for (int64_t tile = first; tile < ntile; tile += nw) {
+        const int64_t nxt = tile + nw;
+        if (nxt < ntile) issue(nxt, stage ^ 1);
+        cp_async_commit();
+        cp_async_wait<1>();
         __syncwarp();
+        const int64_t r0 = tile * 32;
+        const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
         if (lane < nr) {
-            const double2 *mv = reinterpret_cast<const double2 *>(sv + lane * K);
-            const int2 *mc = reinterpret_cast<const int2 *>(sc + lane * K);
-            double acc = 0.0;
+            const double2 *mv = reinterpret_cast<const double2 *>(mine + stage * STB) + lane * (K / 2);
+            const int2 *mc = reinterpret_cast<const int2 *>(mine + stage * STB + VB) + lane * (K / 2);
+            double a0 = 0.0, a1 = 0.0;
 #pragma unroll
             for (int i = 0; i < K / 2; i++) {
-                double2 wv = mv[i];
-                int2 cv = mc[i];
-                acc = fma(wv.x, __ldg(x + cv.x), acc);
-                acc = fma(wv.y, __ldg(x + cv.y), acc);
+                const double2 wv = mv[i];
+                const int2 cv = mc[i];
+                a0 = fma(wv.x, __ldg(x + cv.x), a0);
+                a1 = fma(wv.y, __ldg(x + cv.y), a1);
             }
-            __stcs(y + r0 + lane, acc);
+            __stcs(y + r0 + lane, a0 + a1);
         }
         __syncwarp();
+        stage ^= 1;
     }
+    cp_async_wait<0>();
 }
 
 // Multi-field SpMM: one warp per row, lanes over fields.  X is [cols][F] row-major.
@@ -335,6 +367,33 @@ int blocks_for(int64_t n, int threads, int64_t cap = 65535 * 4)
     return (int)b;
 }
 
+// One CTA of up to 8 warps per SM, each warp with two K-row-tile stages.
+template <int K>
+cudaError_t launch_spmv_pipe(int64_t rows, const int32_t *col, const double *val, const double *x, double *y,
+                             int num_sms, cudaStream_t st)
+{
+    const size_t per_warp = 2 * (size_t)32 * K * 12;
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int wpb = (int)(smem_max / per_warp);
+    if (wpb > 8) wpb = 8;
+    if (wpb < 1) return cudaErrorNotSupported;
+    const size_t smem = per_warp * wpb;
+    cudaError_t e = cudaFuncSetAttribute(spmv_f64_pipe<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmv_f64_pipe<K>, wpb * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+    const int64_t tiles = (rows + 31) / 32;
+    int64_t blocks = (int64_t)num_sms * occ;
+    const int64_t need = (tiles + wpb - 1) / wpb;
+    if (blocks > need) blocks = need;
+    spmv_f64_pipe<K><<<(int)blocks, wpb * 32, smem, st>>>(rows, col, val, x, y);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t *col,
@@ -347,15 +406,13 @@ cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t 
     // `group` carries the uniform stencil size (0 = general CSR)
     switch (group) {
     case 20: spmv_f64_uniform<20><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
-    case 30: {
-        const size_t smem = (size_t)(threads / 32) * 32 * 30 * 12;
-        cudaError_t e = cudaFuncSetAttribute(spmv_f64_staged<30>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        int64_t tiles = (rows + 31) / 32;
-        int sblocks = blocks_for(tiles * 32, threads, (int64_t)num_sms * 2);
-        spmv_f64_staged<30><<<sblocks, threads, smem, st>>>(rows, col, val, x, y);
+    case 30:
+        // cp.async needs 16-byte aligned tiles (true for the library's own arrays)
+        if ((((uintptr_t)val) | ((uintptr_t)col)) & 15u)
+            spmv_f64_uniform<30><<<blocks, threads, 0, st>>>(rows, col, val, x, y);
+        else
+            return launch_spmv_pipe<30>(rows, col, val, x, y, num_sms, st);
         break;
-    }
     case 42: spmv_f64_uniform<42><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
     default: spmv_f64_rows<<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
     }

@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(256) solve_mixed_kernel(SolveArgs a, OpTable o
 
     int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t sys = gw; sys < a.nsys; sys += nw) {
+    for (int64_t ts = gw; ts < a.nsys; ts += nw) {
+        const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
         int j = a.sys_node[sys];
         int n = a.n_node ? a.n_node[j] : a.n;
         int deg = a.deg_node ? a.deg_node[j] : a.deg;

@@ -215,6 +215,102 @@ function calculateneighbors(X, Y, n, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y
     return idxs_x, idxs_y_x, dists_x, dists_y_x
 end
 
-export generate_operator, hyperviscosity_operator, calculateneighbors
+# ----------------------------------------------------------------------------------------
+# Device-resident operators and time stepping (examples/adv_diff_test.jl:144-199).  Field
+# arguments are device buffers: any object whose `pointer` is a device address (a CUDA.jl
+# CuArray, row-major [rows][nfields] as a permuted/transposed view of Julia's column-major
+# storage: `CuArray{Float64}(undef, nfields, rows)`).
+
+struct Problem
+    X::Ptr{Float64}
+    N::Int64
+    Y::Ptr{Float64}
+    M::Int64
+    p::Cint
+    n::Cint
+    polydeg::Cint
+    node_class::Ptr{Int32}
+    n_per_node::Ptr{Int32}
+    deg_per_node::Ptr{Int32}
+    op_mask::UInt32
+    k_deriv::Cint
+    precision::Cint
+    memspace::Cint
+    row_begin::Int64
+    row_end::Int64
+end
+
+devptr(a) = reinterpret(Ptr{Cvoid}, UInt(pointer(a)))
+
+mutable struct OperatorSet
+    ptr::Ptr{Cvoid}
+    h::Handle
+    ops::Vector{Symbol}
+end
+
+"Operators `ops` of the collocated node set X kept in GPU memory (rbffd_opset_create)."
+function OperatorSet(X, p, n, polydeg, ops; precision = :mixed, k_deriv = 0, node_class = nothing, h = handle())
+    Xv = points(X)
+    order = sort(collect(ops); by = o -> getfield(OP, o))
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    stats = Ref(Stats())
+    GC.@preserve Xv node_class begin
+        prob = Ref(Problem(pointer(reinterpret(Float64, Xv)), length(Xv), C_NULL, 0, p, n, polydeg,
+                           node_class === nothing ? C_NULL : pointer(node_class), C_NULL, C_NULL, mask(order),
+                           k_deriv, getfield(PREC, precision), 0, 0, 0))
+        rc = ccall((:rbffd_opset_create, LIB), Cint, (Ptr{Cvoid}, Ref{Problem}, Ref{Ptr{Cvoid}}, Ref{Stats}),
+                   h.ptr, prob, ref, stats)
+    end
+    check(h, rc, stats)
+    s = OperatorSet(ref[], h, order)
+    finalizer(x -> (x.ptr == C_NULL || ccall((:rbffd_opset_destroy, LIB), Cvoid, (Ptr{Cvoid}, Ptr{Cvoid}),
+                                             x.h.ptr, x.ptr); x.ptr = C_NULL), s)
+    return s
+end
+
+"y = A_op x on the GPU (x, y device vectors of Float64), the `D * u` of cons_sys."
+function spmv!(y, s::OperatorSet, op::Symbol, x)
+    q = findfirst(==(op), s.ops) - 1
+    rc = ccall((:rbffd_spmv, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
+               s.h.ptr, s.ptr, q, devptr(x), devptr(y))
+    check(s.h, rc, Ref(Stats()))
+    return y
+end
+
+mutable struct RK4
+    ptr::Ptr{Cvoid}
+    h::Handle
+    sets::Vector{OperatorSet}
+end
+
+"RK4 for du/dt = L u, L = sum(coef .* operators of `sets`); rows with fixed_rows[i] != 0 held."
+function RK4(sets::Vector{OperatorSet}, coef::Vector{Float64}, nfields; fixed_rows = nothing, dtype = :f64)
+    h = sets[1].h
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    ptrs = [s.ptr for s in sets]
+    fx = fixed_rows === nothing ? nothing : UInt8.(fixed_rows .!= 0)
+    GC.@preserve ptrs coef fx begin
+        rc = ccall((:rbffd_rk4_create, LIB), Cint,
+                   (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Cint, Ptr{Float64}, Ptr{UInt8}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                   h.ptr, pointer(ptrs), length(sets), pointer(coef), fx === nothing ? C_NULL : pointer(fx),
+                   nfields, dtype === :f64 ? 0 : 1, ref)
+    end
+    check(h, rc, Ref(Stats()))
+    rk = RK4(ref[], h, sets)
+    finalizer(x -> (x.ptr == C_NULL || ccall((:rbffd_rk4_destroy, LIB), Cvoid, (Ptr{Cvoid}, Ptr{Cvoid}),
+                                             x.h.ptr, x.ptr); x.ptr = C_NULL), rk)
+    return rk
+end
+
+"Advance the device fields u in place by nsteps RK4 steps of size dt."
+function step!(rk::RK4, u, dt, nsteps)
+    rc = ccall((:rbffd_rk4_run, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Int64),
+               rk.h.ptr, rk.ptr, devptr(u), dt, nsteps)
+    check(rk.h, rc, Ref(Stats()))
+    ccall((:rbffd_synchronize, LIB), Cint, (Ptr{Cvoid},), rk.h.ptr)
+    return u
+end
+
+export generate_operator, hyperviscosity_operator, calculateneighbors, OperatorSet, spmv!, RK4, step!
 
 end # module

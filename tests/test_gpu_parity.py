@@ -253,6 +253,23 @@ def test_spmv_and_spmm(pkg, orc, gpu):
         assert np.abs(y32.cpu().numpy() - yr).max() <= 1e-4 * np.abs(yr).max()
 
 
+def test_spmv_pipelined_tiles(pkg, gpu):
+    """k = 30 takes the cp.async two-stage SpMV: 90,000 rows = 2812 full 32-row tiles plus a
+    partial one, several tiles per warp (both stages reused), against scipy's CSR product."""
+    import torch
+
+    X, _ = grid(pkg, 300, seed=8)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(len(X))
+    with pkg.OperatorSet(X, None, 3, 30, 3, ops=("Dx", "Lap")) as s:
+        xd = torch.tensor(x, device="cuda")
+        yd = torch.empty_like(xd)
+        for o in ("Dx", "Lap"):
+            s.spmv(o, xd, yd)
+            yr = s.csr(o) @ x
+            assert np.abs(yd.cpu().numpy() - yr).max() <= 1e-12 * np.abs(yr).max(), o
+
+
 def test_row_range_shards(pkg, orc, gpu):
     X, _ = grid(pkg, 40, seed=4)
     p, n, deg = 3, 20, 3
