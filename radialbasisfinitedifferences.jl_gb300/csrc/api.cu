@@ -35,6 +35,8 @@ struct rbffd_opset {
     int32_t *col = nullptr;
     double *val = nullptr;
     float *val32 = nullptr;
+    int32_t *sell_col = nullptr;  // SELL-32 copy for the SpMV (uniform stencils), built on first use
+    double *sell_val = nullptr;
     int64_t *csc_colptr = nullptr, *csc_rowval = nullptr, *csc_perm = nullptr;
     double *csc_tmp = nullptr;
     std::vector<void *> owned;
@@ -960,9 +962,24 @@ RBFFD_EXPORT int rbffd_spmv(rbffd_handle *h, rbffd_opset *s, int op, const doubl
 {
     if (!h) return RBFFD_EINVAL;
     if (!s || op < 0 || op >= s->nops || !x || !y) return fail(h, RBFFD_EINVAL, "bad spmv arguments");
-    int kuni = s->uniform ? s->n : 0;  // uniform-stencil kernels need row r at r * n
-    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, kuni, h->num_sms,
-                       h->stream));
+    if (s->uniform) {
+        const int64_t padded = sell_padded(s->rows, s->n);
+        if (!s->sell_val) {
+            int32_t *sc;
+            double *sv;
+            CK(cudaMallocAsync((void **)&sc, (size_t)padded * sizeof(int32_t), h->stream));
+            s->owned.push_back(sc);
+            CK(cudaMallocAsync((void **)&sv, (size_t)padded * s->nops * sizeof(double), h->stream));
+            s->owned.push_back(sv);
+            CK(launch_csr_to_sell(s->rows, s->n, s->col, s->val, s->nops, s->nnz, sc, sv, h->stream));
+            s->sell_col = sc;
+            s->sell_val = sv;
+        }
+        CK(launch_spmv_sell(s->rows, s->n, s->sell_col, s->sell_val + (size_t)op * padded, x, y, h->num_sms,
+                            h->stream));
+        return RBFFD_OK;
+    }
+    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, 0, h->num_sms, h->stream));
     return RBFFD_OK;
 }
 
@@ -998,6 +1015,7 @@ struct rbffd_rk4 {
     double *val64 = nullptr;
     float *val32 = nullptr;
     uint8_t *fixed = nullptr;
+    int32_t *order = nullptr;  // rows in Morton (Z-curve) order of their nodes
     void *unext = nullptr, *wA = nullptr, *wB = nullptr, *acc = nullptr;
     cudaGraphExec_t graph2 = nullptr;  // two steps u -> unext -> u
     const void *graph_u = nullptr;
@@ -1011,16 +1029,16 @@ cudaError_t rk4_enqueue_step(rbffd_handle *h, rbffd_rk4 *rk, const void *u, void
 {
     const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
     cudaError_t e;
-    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, u, u, rk->acc, rk->wA, rk->fixed, rk->F, 0.5 * dt, 0,
+    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, u, u, rk->acc, rk->wA, rk->fixed, rk->F, 0.5 * dt, 0,
                          rk->dtype, h->num_sms, st);
     if (e != cudaSuccess) return e;
-    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, rk->wB, rk->fixed, rk->F, 0.5 * dt,
+    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, rk->wB, rk->fixed, rk->F, 0.5 * dt,
                          1, rk->dtype, h->num_sms, st);
     if (e != cudaSuccess) return e;
-    e = launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wB, u, rk->acc, rk->wA, rk->fixed, rk->F, dt, 1,
+    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wB, u, rk->acc, rk->wA, rk->fixed, rk->F, dt, 1,
                          rk->dtype, h->num_sms, st);
     if (e != cudaSuccess) return e;
-    return launch_rk4_stage(rk->rows, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, out, rk->fixed, rk->F, dt / 6.0,
+    return launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, out, rk->fixed, rk->F, dt / 6.0,
                             2, rk->dtype, h->num_sms, st);
 }
 }  // namespace
@@ -1082,6 +1100,40 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
     CKB(cudaMemcpyAsync(rk->row_ptr, s0->row_ptr, sizeof(int64_t) * (rk->rows + 1), cudaMemcpyDeviceToDevice, st));
     CKB(cudaMemcpyAsync(rk->col, s0->col, sizeof(int32_t) * rk->nnz, cudaMemcpyDeviceToDevice, st));
     CKB(launch_combine_ops(rk->nnz, dvals, dcoef, nq, rk->val64, rk->val32, st));
+    {
+        // Z-curve order of the nodes (16 bits per axis over the bounding box): consecutive
+        // rows of the order are spatial neighbours, so the stage kernel's gathers hit L1
+        std::vector<double2> hx(rk->rows);
+        CKB(cudaMemcpyAsync(hx.data(), s0->X, sizeof(double2) * rk->rows, cudaMemcpyDeviceToHost, st));
+        CKB(cudaStreamSynchronize(st));
+        double x0 = hx[0].x, x1 = hx[0].x, y0 = hx[0].y, y1 = hx[0].y;
+        for (const double2 &q : hx) {
+            x0 = std::min(x0, q.x);
+            x1 = std::max(x1, q.x);
+            y0 = std::min(y0, q.y);
+            y1 = std::max(y1, q.y);
+        }
+        const double sxq = x1 > x0 ? 65535.0 / (x1 - x0) : 0.0, syq = y1 > y0 ? 65535.0 / (y1 - y0) : 0.0;
+        auto spread = [](uint32_t v) {
+            uint64_t z = v & 0xffffu;
+            z = (z | (z << 8)) & 0x00ff00ffu;
+            z = (z | (z << 4)) & 0x0f0f0f0fu;
+            z = (z | (z << 2)) & 0x33333333u;
+            z = (z | (z << 1)) & 0x55555555u;
+            return z;
+        };
+        std::vector<std::pair<uint64_t, int32_t>> kv(rk->rows);
+        for (int64_t i = 0; i < rk->rows; i++) {
+            const uint32_t qx = (uint32_t)((hx[i].x - x0) * sxq), qy = (uint32_t)((hx[i].y - y0) * syq);
+            kv[i] = {spread(qx) | (spread(qy) << 1), (int32_t)i};
+        }
+        std::sort(kv.begin(), kv.end());
+        std::vector<int32_t> ho(rk->rows);
+        for (int64_t i = 0; i < rk->rows; i++) ho[i] = kv[i].second;
+        CKB(keep.get(&rk->order, rk->rows));
+        CKB(cudaMemcpyAsync(rk->order, ho.data(), sizeof(int32_t) * rk->rows, cudaMemcpyHostToDevice, st));
+        CKB(cudaStreamSynchronize(st));
+    }
     if (fixed_rows) {
         CKB(keep.get(&rk->fixed, rk->rows));
         CKB(cudaMemcpyAsync(rk->fixed, fixed_rows, rk->rows, cudaMemcpyHostToDevice, st));

@@ -157,9 +157,15 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
                         const void *val, const void *x, void *y, int nfields, int dtype,
                         cudaStream_t st);
 // RK4 stage (mode 0: first stage, 1: middle stages, 2: last stage), see sparse.cu.
-cudaError_t launch_rk4_stage(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
-                             const void *w, const void *u, void *acc, void *out, const uint8_t *fixed, int F,
-                             double c, int mode, int dtype, int num_sms, cudaStream_t st);
+// SELL-32 copy of a uniform-stencil operator set (all operators) and the SpMV on it.
+int64_t sell_padded(int64_t rows, int K);
+cudaError_t launch_csr_to_sell(int64_t rows, int K, const int32_t *col, const double *val, int nops, int64_t nnz,
+                               int32_t *scol, double *sval, cudaStream_t st);
+cudaError_t launch_spmv_sell(int64_t rows, int K, const int32_t *scol, const double *sval, const double *x, double *y,
+                             int num_sms, cudaStream_t st);
+cudaError_t launch_rk4_stage(int64_t rows, const int32_t *order, const int64_t *row_ptr, const int32_t *col,
+                             const void *val, const void *w, const void *u, void *acc, void *out,
+                             const uint8_t *fixed, int F, double c, int mode, int dtype, int num_sms, cudaStream_t st);
 cudaError_t launch_combine_ops(int64_t nnz, const double *const *vals, const double *coef, int nq,
                                double *out64, float *out32, cudaStream_t st);
 cudaError_t launch_count_diff(int64_t n, const int32_t *a, const int32_t *b, unsigned long long *cnt,

@@ -79,13 +79,75 @@ __device__ __forceinline__ void cp_async_wait()
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Uniform stencil size K (even), two-stage pipeline: each warp owns tiles of 32 consecutive
-// rows (weights 32*K doubles and column ids 32*K ints, contiguous and 16-byte aligned in HBM)
-// and copies the next tile into its second shared-memory stage with cp.async while it
-// computes the current one, so HBM streaming overlaps the FP64 FMAs (31.5M FMAs take ~50 us
-// at GB300's FP64 rate, about as long as streaming their 378 MB).  Each lane accumulates its
-// own row from shared memory in two independent chains; x is gathered through L1/L2.
+// SELL-32 layout of a uniform-stencil operator (sliced ELLPACK with slice height 32, one warp):
+// slice (tile) i holds rows 32i..32i+31 column-major, entry t of row 32i + l at
+// (i*K + t)*32 + l, so the t-th weights and column ids of a warp's 32 rows are one contiguous
+// 256-byte / 128-byte line.  Rows past the end are padded with weight 0 and column 0.
+__global__ void __launch_bounds__(256) csr_to_sell_kernel(int64_t rows, int K, const int32_t *__restrict__ col,
+                                                          const double *__restrict__ val, int nops, int64_t nnz,
+                                                          int64_t padded, int32_t *__restrict__ scol,
+                                                          double *__restrict__ sval)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t ntile = (rows + 31) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; tile < ntile; tile += nw) {
+        const int64_t r = tile * 32 + lane;
+        const bool ok = r < rows;
+        const int64_t src = (ok ? r : 0) * K, dst = tile * 32 * K + lane;
+        for (int t = 0; t < K; t++) scol[dst + 32 * t] = ok ? col[src + t] : 0;
+        for (int q = 0; q < nops; q++)
+            for (int t = 0; t < K; t++) sval[q * padded + dst + 32 * t] = ok ? val[q * nnz + src + t] : 0.0;
+    }
+}
+
+// FP64 SpMV on the SELL-32 layout: warp per 32-row slice, lane per row.  Every weight and
+// column-id load is a fully coalesced line, so no shared-memory staging is needed and the
+// kernel runs at full occupancy (the latency of the x gathers is hidden by warps, not
+// stages); each row accumulates in four independent FP64 chains.
 template <int K>
+__global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const int32_t *__restrict__ scol,
+                                                     const double *__restrict__ sval, const double *__restrict__ x,
+                                                     double *__restrict__ y)
+{
+    const int k = K > 0 ? K : kr;
+    const int lane = threadIdx.x & 31;
+    const int64_t ntile = (rows + 31) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; tile < ntile; tile += nw) {
+        const int32_t *c = scol + tile * 32 * k + lane;
+        const double *v = sval + tile * 32 * k + lane;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        if constexpr (K > 0) {
+#pragma unroll
+            for (int t = 0; t < K; t++) a[t & 3] = fma(__ldcs(v + 32 * t), __ldg(x + __ldcs(c + 32 * t)), a[t & 3]);
+        } else {
+            int t = 0;
+            for (; t + 4 <= k; t += 4) {
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    a[u] = fma(__ldcs(v + 32 * (t + u)), __ldg(x + __ldcs(c + 32 * (t + u))), a[u]);
+            }
+            for (; t < k; t++) a[0] = fma(__ldcs(v + 32 * t), __ldg(x + __ldcs(c + 32 * t)), a[0]);
+        }
+        const int64_t r = tile * 32 + lane;
+        if (r < rows) __stcs(y + r, (a[0] + a[1]) + (a[2] + a[3]));
+    }
+}
+
+// Pipeline depth of the FP64 SpMV (tiles in flight per warp, including the one computed).
+#ifndef RBFFD_SPMV_STAGES
+#define RBFFD_SPMV_STAGES 3
+#endif
+
+// Uniform stencil size K (even), S-stage pipeline: each warp owns tiles of 32 consecutive
+// rows (weights 32*K doubles and column ids 32*K ints, contiguous and 16-byte aligned in HBM)
+// and keeps the next S-1 tiles in flight into its shared-memory stages with cp.async while
+// it computes the current one, so HBM streaming overlaps the FP64 FMAs (31.5M FMAs take
+// ~50 us at GB300's FP64 rate, about as long as streaming their 378 MB).  Each lane
+// accumulates its own row from shared memory in four independent chains; x is gathered
+// through L1/L2.
+template <int K, int S>
 __global__ void __launch_bounds__(256) spmv_f64_pipe(int64_t rows, const int32_t *__restrict__ col,
                                                      const double *__restrict__ val,
                                                      const double *__restrict__ x, double *__restrict__ y)
@@ -94,7 +156,7 @@ __global__ void __launch_bounds__(256) spmv_f64_pipe(int64_t rows, const int32_t
     constexpr int VB = 32 * K * 8, CB = 32 * K * 4, STB = VB + CB;
     extern __shared__ __align__(16) unsigned char sm_dyn[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned char *mine = sm_dyn + (size_t)w * 2 * STB;
+    unsigned char *mine = sm_dyn + (size_t)w * S * STB;
     unsigned long long pol;
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
     const int64_t ntile = (rows + 31) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -114,34 +176,67 @@ __global__ void __launch_bounds__(256) spmv_f64_pipe(int64_t rows, const int32_t
         for (int c = 4 * nc4 + lane; c < nc; c += 32) sc[c] = __ldcs(col + r0 * K + c);
     };
 
-    if (first < ntile) issue(first, 0);
-    cp_async_commit();
+#pragma unroll
+    for (int k = 0; k < S - 1; k++) {
+        const int64_t t = first + k * nw;
+        if (t < ntile) issue(t, k);
+        cp_async_commit();
+    }
     int stage = 0;
     for (int64_t tile = first; tile < ntile; tile += nw) {
-        const int64_t nxt = tile + nw;
-        if (nxt < ntile) issue(nxt, stage ^ 1);
+        const int64_t nxt = tile + (S - 1) * nw;
+        if (nxt < ntile) issue(nxt, stage == 0 ? S - 1 : stage - 1);
         cp_async_commit();
-        cp_async_wait<1>();
+        cp_async_wait<S - 1>();
         __syncwarp();
         const int64_t r0 = tile * 32;
         const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
         if (lane < nr) {
             const double2 *mv = reinterpret_cast<const double2 *>(mine + stage * STB) + lane * (K / 2);
             const int2 *mc = reinterpret_cast<const int2 *>(mine + stage * STB + VB) + lane * (K / 2);
-            double a0 = 0.0, a1 = 0.0;
+            double a[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
             for (int i = 0; i < K / 2; i++) {
                 const double2 wv = mv[i];
                 const int2 cv = mc[i];
-                a0 = fma(wv.x, __ldg(x + cv.x), a0);
-                a1 = fma(wv.y, __ldg(x + cv.y), a1);
+                a[(2 * i) & 3] = fma(wv.x, __ldg(x + cv.x), a[(2 * i) & 3]);
+                a[(2 * i + 1) & 3] = fma(wv.y, __ldg(x + cv.y), a[(2 * i + 1) & 3]);
             }
-            __stcs(y + r0 + lane, a0 + a1);
+            __stcs(y + r0 + lane, (a[0] + a[1]) + (a[2] + a[3]));
         }
         __syncwarp();
-        stage ^= 1;
+        stage = stage == S - 1 ? 0 : stage + 1;
     }
     cp_async_wait<0>();
+}
+
+// v[f] = sum_t val[t] x[col[t]][f] for one row, lanes over fields f = f0 + lane and f0 + lane + 32:
+// the row's column ids and weights are loaded once, coalesced (lane t holds entry t), and
+// broadcast by shuffles, so the x gathers do not wait on dependent index loads.
+template <typename T>
+__device__ __forceinline__ void row_fields(int64_t a, int len, const int32_t *__restrict__ col,
+                                           const T *__restrict__ val, const T *__restrict__ x, int F, int f0,
+                                           int lane, T &v0, T &v1)
+{
+    const int f = f0 + lane, g = f + 32;
+    for (int t0 = 0; t0 < len; t0 += 32) {
+        const int tl = t0 + lane;
+        int cl = 0;
+        T wl = 0;
+        if (tl < len) {
+            cl = __ldg(col + a + tl);
+            wl = __ldg(val + a + tl);
+        }
+        const int cnt = len - t0 < 32 ? len - t0 : 32;
+#pragma unroll 6
+        for (int t = 0; t < cnt; t++) {
+            const int cc = __shfl_sync(0xffffffffu, cl, t);
+            const T wt = __shfl_sync(0xffffffffu, wl, t);
+            const T *xr = x + (int64_t)cc * F;
+            if (f < F) v0 = fma(wt, __ldg(xr + f), v0);
+            if (g < F) v1 = fma(wt, __ldg(xr + g), v1);
+        }
+    }
 }
 
 // Multi-field SpMM: one warp per row, lanes over fields.  X is [cols][F] row-major.
@@ -151,80 +246,76 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t rows, const int64_t *
                                                    const T *__restrict__ val,
                                                    const T *__restrict__ x, T *__restrict__ y, int F)
 {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = warp; r < rows; r += nw) {
-        int64_t a = row_ptr[r], b = row_ptr[r + 1];
+        const int64_t a = row_ptr[r];
+        const int len = (int)(row_ptr[r + 1] - a);
         for (int f0 = 0; f0 < F; f0 += 64) {
-            T acc0 = 0, acc1 = 0;
-            int f = f0 + lane;
-            for (int64_t t = a; t < b; t++) {
-                T w = val[t];
-                int64_t c = col[t];
-                const T *xr = x + c * F;
-                if (f < F) acc0 = fma(w, xr[f], acc0);
-                if (f + 32 < F) acc1 = fma(w, xr[f + 32], acc1);
-            }
-            if (f < F) y[r * F + f] = acc0;
-            if (f + 32 < F) y[r * F + f + 32] = acc1;
+            T v0 = 0, v1 = 0;
+            row_fields<T>(a, len, col, val, x, F, f0, lane, v0, v1);
+            const int f = f0 + lane, g = f + 32;
+            if (f < F) y[r * F + f] = v0;
+            if (g < F) y[r * F + g] = v1;
         }
     }
 }
 
 // One RK4 stage of du/dt = L u on F fields (classic RK4; examples/adv_diff_test.jl solves the
-// same semi-discrete system with SSPRK43).  v = L w for every row (warp per row, lanes over
-// fields), v = 0 on fixed rows (held at their initial values, the Dirichlet overwrite of
-// examples/adv_diff_test.jl:166-167), then the epilogue folds the RK bookkeeping in, so no
-// stage derivative is stored:
+// same semi-discrete system with SSPRK43).  v = L w for every row, v = 0 on fixed rows (held
+// at their initial values, the Dirichlet overwrite of examples/adv_diff_test.jl:166-167),
+// then the epilogue folds the RK bookkeeping in, so no stage derivative is stored:
 //   mode 0 (stage 1): acc  = v;          wnext = u + c v
 //   mode 1 (stage 2, 3): acc += 2 v;     wnext = u + c v
 //   mode 2 (stage 4): unext = u + c (acc + v)        (c = dt / 6)
+// Rows are visited in `order` (a spatial locality order of the nodes): a CTA takes chunks of
+// 64 consecutive rows of that order and its 8 warps work on neighbouring rows together, so the
+// gathered rows of w (F values each) are shared through L1 instead of being re-read from L2.
 template <typename T>
-__global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
+__global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int32_t *__restrict__ order,
+                                                        const int64_t *__restrict__ row_ptr,
                                                         const int32_t *__restrict__ col, const T *__restrict__ val,
                                                         const T *__restrict__ w, const T *__restrict__ u,
                                                         T *__restrict__ acc, T *__restrict__ out,
                                                         const uint8_t *__restrict__ fixed, int F, T c, int mode)
 {
-    const int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < rows; r += nw) {
-        const int64_t a = row_ptr[r], b = row_ptr[r + 1];
-        const bool fx = fixed && fixed[r];
-        for (int f0 = 0; f0 < F; f0 += 64) {
-            const int f = f0 + lane, g = f + 32;
-            T v0 = 0, v1 = 0;
-            if (!fx) {
-                for (int64_t t = a; t < b; t++) {
-                    const T wt = val[t];
-                    const T *xr = w + (int64_t)col[t] * F;
-                    if (f < F) v0 = fma(wt, xr[f], v0);
-                    if (g < F) v1 = fma(wt, xr[g], v1);
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t nchunk = (rows + 63) >> 6;
+    for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        for (int k = 0; k < 8; k++) {
+            const int64_t idx = ch * 64 + k * 8 + wib;
+            if (idx >= rows) break;
+            const int64_t r = order ? (int64_t)order[idx] : idx;
+            const int64_t a = row_ptr[r];
+            const int len = (int)(row_ptr[r + 1] - a);
+            const bool fx = fixed && fixed[r];
+            for (int f0 = 0; f0 < F; f0 += 64) {
+                const int f = f0 + lane, g = f + 32;
+                T v0 = 0, v1 = 0;
+                if (!fx) row_fields<T>(a, len, col, val, w, F, f0, lane, v0, v1);
+                const int64_t o = r * F;
+                if (f < F) {
+                    if (mode == 0) {
+                        acc[o + f] = v0;
+                        out[o + f] = fma(c, v0, u[o + f]);
+                    } else if (mode == 1) {
+                        acc[o + f] = fma((T)2, v0, acc[o + f]);
+                        out[o + f] = fma(c, v0, u[o + f]);
+                    } else {
+                        out[o + f] = fma(c, acc[o + f] + v0, u[o + f]);
+                    }
                 }
-            }
-            const int64_t o = r * F;
-            if (f < F) {
-                if (mode == 0) {
-                    acc[o + f] = v0;
-                    out[o + f] = fma(c, v0, u[o + f]);
-                } else if (mode == 1) {
-                    acc[o + f] = fma((T)2, v0, acc[o + f]);
-                    out[o + f] = fma(c, v0, u[o + f]);
-                } else {
-                    out[o + f] = fma(c, acc[o + f] + v0, u[o + f]);
-                }
-            }
-            if (g < F) {
-                if (mode == 0) {
-                    acc[o + g] = v1;
-                    out[o + g] = fma(c, v1, u[o + g]);
-                } else if (mode == 1) {
-                    acc[o + g] = fma((T)2, v1, acc[o + g]);
-                    out[o + g] = fma(c, v1, u[o + g]);
-                } else {
-                    out[o + g] = fma(c, acc[o + g] + v1, u[o + g]);
+                if (g < F) {
+                    if (mode == 0) {
+                        acc[o + g] = v1;
+                        out[o + g] = fma(c, v1, u[o + g]);
+                    } else if (mode == 1) {
+                        acc[o + g] = fma((T)2, v1, acc[o + g]);
+                        out[o + g] = fma(c, v1, u[o + g]);
+                    } else {
+                        out[o + g] = fma(c, acc[o + g] + v1, u[o + g]);
+                    }
                 }
             }
         }
@@ -367,12 +458,13 @@ int blocks_for(int64_t n, int threads, int64_t cap = 65535 * 4)
     return (int)b;
 }
 
-// One CTA of up to 8 warps per SM, each warp with two K-row-tile stages.
+// One CTA of up to 8 warps per SM, each warp with RBFFD_SPMV_STAGES K-row-tile stages.
 template <int K>
 cudaError_t launch_spmv_pipe(int64_t rows, const int32_t *col, const double *val, const double *x, double *y,
                              int num_sms, cudaStream_t st)
 {
-    const size_t per_warp = 2 * (size_t)32 * K * 12;
+    constexpr int S = RBFFD_SPMV_STAGES;
+    const size_t per_warp = S * (size_t)32 * K * 12;
     int dev = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -380,17 +472,18 @@ cudaError_t launch_spmv_pipe(int64_t rows, const int32_t *col, const double *val
     if (wpb > 8) wpb = 8;
     if (wpb < 1) return cudaErrorNotSupported;
     const size_t smem = per_warp * wpb;
-    cudaError_t e = cudaFuncSetAttribute(spmv_f64_pipe<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = spmv_f64_pipe<K, S>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmv_f64_pipe<K>, wpb * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, wpb * 32, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
     const int64_t tiles = (rows + 31) / 32;
     int64_t blocks = (int64_t)num_sms * occ;
     const int64_t need = (tiles + wpb - 1) / wpb;
     if (blocks > need) blocks = need;
-    spmv_f64_pipe<K><<<(int)blocks, wpb * 32, smem, st>>>(rows, col, val, x, y);
+    kern<<<(int)blocks, wpb * 32, smem, st>>>(rows, col, val, x, y);
     return cudaGetLastError();
 }
 
@@ -419,6 +512,31 @@ cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t 
     return cudaGetLastError();
 }
 
+int64_t sell_padded(int64_t rows, int K) { return ((rows + 31) / 32) * 32 * (int64_t)K; }
+
+cudaError_t launch_csr_to_sell(int64_t rows, int K, const int32_t *col, const double *val, int nops, int64_t nnz,
+                               int32_t *scol, double *sval, cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    const int64_t ntile = (rows + 31) / 32;
+    csr_to_sell_kernel<<<blocks_for(ntile * 32, 256), 256, 0, st>>>(rows, K, col, val, nops, nnz,
+                                                                     sell_padded(rows, K), scol, sval);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spmv_sell(int64_t rows, int K, const int32_t *scol, const double *sval, const double *x, double *y,
+                             int num_sms, cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    const int64_t ntile = (rows + 31) / 32;
+    const int blocks = blocks_for(ntile * 32, 256, (int64_t)num_sms * 8);
+    if (K == 30)
+        spmv_f64_sell<30><<<blocks, 256, 0, st>>>(rows, K, scol, sval, x, y);
+    else
+        spmv_f64_sell<0><<<blocks, 256, 0, st>>>(rows, K, scol, sval, x, y);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
                         const void *x, void *y, int nfields, int dtype, cudaStream_t st)
 {
@@ -434,18 +552,18 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
     return cudaGetLastError();
 }
 
-cudaError_t launch_rk4_stage(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
-                             const void *w, const void *u, void *acc, void *out, const uint8_t *fixed, int F,
-                             double c, int mode, int dtype, int num_sms, cudaStream_t st)
+cudaError_t launch_rk4_stage(int64_t rows, const int32_t *order, const int64_t *row_ptr, const int32_t *col,
+                             const void *val, const void *w, const void *u, void *acc, void *out,
+                             const uint8_t *fixed, int F, double c, int mode, int dtype, int num_sms, cudaStream_t st)
 {
     if (rows <= 0) return cudaSuccess;
-    int blocks = blocks_for(rows * 32, 256, (int64_t)num_sms * 8);
+    int blocks = blocks_for((rows + 63) / 64, 1, (int64_t)num_sms * 8);
     if (dtype == 0)
-        rk4_stage_kernel<double><<<blocks, 256, 0, st>>>(rows, row_ptr, col, (const double *)val, (const double *)w,
+        rk4_stage_kernel<double><<<blocks, 256, 0, st>>>(rows, order, row_ptr, col, (const double *)val, (const double *)w,
                                                          (const double *)u, (double *)acc, (double *)out, fixed, F, c,
                                                          mode);
     else
-        rk4_stage_kernel<float><<<blocks, 256, 0, st>>>(rows, row_ptr, col, (const float *)val, (const float *)w,
+        rk4_stage_kernel<float><<<blocks, 256, 0, st>>>(rows, order, row_ptr, col, (const float *)val, (const float *)w,
                                                         (const float *)u, (float *)acc, (float *)out, fixed, F,
                                                         (float)c, mode);
     return cudaGetLastError();

@@ -253,9 +253,9 @@ def test_spmv_and_spmm(pkg, orc, gpu):
         assert np.abs(y32.cpu().numpy() - yr).max() <= 1e-4 * np.abs(yr).max()
 
 
-def test_spmv_pipelined_tiles(pkg, gpu):
-    """k = 30 takes the cp.async two-stage SpMV: 90,000 rows = 2812 full 32-row tiles plus a
-    partial one, several tiles per warp (both stages reused), against scipy's CSR product."""
+def test_spmv_sell_tiles(pkg, gpu):
+    """k = 30 takes the SELL-32 SpMV: 90,000 rows = 2812 full 32-row slices plus a padded
+    partial one, several slices per warp, against scipy's CSR product."""
     import torch
 
     X, _ = grid(pkg, 300, seed=8)
