@@ -38,6 +38,10 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 #ifndef RBFFD_SCHUR_MIN_BLOCKS
 #define RBFFD_SCHUR_MIN_BLOCKS 4
 #endif
+// 1: the FP64 Phi passes run inside the first Gauss-Jordan steps (see reg_gj's hook).
+#ifndef RBFFD_SCHUR_INTERLEAVE
+#define RBFFD_SCHUR_INTERLEAVE 1
+#endif
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
 template <int B, int E, typename F>
@@ -167,14 +171,22 @@ __device__ __forceinline__ void fill_phi_rows(RegRows<SP> &R, const float2 *x32,
 // row stays multiplied by its pivot (elimination is linear, so later updates apply unchanged)
 // and is divided by it once at the end, so each step is a uniform FMA sweep.  Fails on a
 // zero, subnormal, infinite or NaN pivot.
-template <int S>
-__device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *dinv, float *prow, int lane)
+struct NoHook {
+    __device__ void operator()(int) const {}
+};
+
+// `hook(c)` runs at the start of steps c < 8: independent work (the FP64 assembly) placed
+// there overlaps the latency of the elimination's FP32 chain.
+template <int S, typename Hook = NoHook>
+__device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *dinv, float *prow, int lane,
+                                       Hook &&hook = Hook())
 {
     constexpr int NS = RegRows<S>::NS;
     bool ok = true;
     static_for<0, S>([&](auto CC) {
         constexpr int c = decltype(CC)::value;
         if (c >= s || !ok) return;
+        if constexpr (c < 8) hook(c);  // the first 8 steps only: bounded code size
         unsigned key = 0u;
         int brow = INT_MAX;
 #pragma unroll
@@ -527,30 +539,38 @@ __device__ __forceinline__ void residual_schur(const double *phiP, const double 
     __syncwarp();
 }
 
-// Packed FP64 Phi (two pairs per lane per pass) and FP64 P rows.
-__device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
-                                                    double *P, int lane)
+// One pass of the packed FP64 Phi: strictly lower pairs t0 + lane and t0 + 32 + lane
+// (row-major: t = i (i - 1) / 2 + j, stored at tri_off(i) + j = t + i).
+__device__ __forceinline__ void phi_pair_pass(const double *xs, int n, int p, double *phiP, int t0, int lane)
 {
-    const int npairs = n * (n - 1) / 2;  // strictly lower pairs, row-major: t = i (i - 1) / 2 + j
-    for (int t = lane; t < npairs; t += 64) {
-        const int t2 = t + 32;
-        const bool two = t2 < npairs;
-        int i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)t)) * 0.5f);
-        if ((i * (i - 1)) / 2 > t) i--;
-        if (((i + 1) * i) / 2 <= t) i++;
-        const int j = t - (i * (i - 1)) / 2;
-        const int tt = two ? t2 : t;
-        int i2 = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)tt)) * 0.5f);
-        if ((i2 * (i2 - 1)) / 2 > tt) i2--;
-        if (((i2 + 1) * i2) / 2 <= tt) i2++;
-        const int j2 = tt - (i2 * (i2 - 1)) / 2;
-        const double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
-        const double dx2 = xs[2 * i2] - xs[2 * j2], dy2 = xs[2 * i2 + 1] - xs[2 * j2 + 1];
-        const double v = phi64_nr(fma(dx, dx, dy * dy), p);
-        const double v2 = phi64_nr(fma(dx2, dx2, dy2 * dy2), p);
-        phiP[t + i] = v;  // tri_off(i) + j = t + i
-        if (two) phiP[tt + i2] = v2;
-    }
+    const int npairs = n * (n - 1) / 2;
+    const int t = t0 + lane;
+    if (t >= npairs) return;
+    const int t2 = t + 32;
+    const bool two = t2 < npairs;
+    int i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)t)) * 0.5f);
+    if ((i * (i - 1)) / 2 > t) i--;
+    if (((i + 1) * i) / 2 <= t) i++;
+    const int j = t - (i * (i - 1)) / 2;
+    const int tt = two ? t2 : t;
+    int i2 = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)tt)) * 0.5f);
+    if ((i2 * (i2 - 1)) / 2 > tt) i2--;
+    if (((i2 + 1) * i2) / 2 <= tt) i2++;
+    const int j2 = tt - (i2 * (i2 - 1)) / 2;
+    const double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
+    const double dx2 = xs[2 * i2] - xs[2 * j2], dy2 = xs[2 * i2 + 1] - xs[2 * j2 + 1];
+    const double v = phi64_nr(fma(dx, dx, dy * dy), p);
+    const double v2 = phi64_nr(fma(dx2, dx2, dy2 * dy2), p);
+    phiP[t + i] = v;
+    if (two) phiP[tt + i2] = v2;
+}
+
+// Passes [pass0, end) of the packed FP64 Phi, its zero diagonal and the FP64 P rows.
+__device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
+                                                    double *P, int pass0, int lane)
+{
+    const int npass = (n * (n - 1) / 2 + 63) / 64;
+    for (int q = pass0; q < npass; q++) phi_pair_pass(xs, n, p, phiP, 64 * q, lane);
     for (int i = lane; i < n; i += 32) {
         phiP[tri_off(i) + i] = 0.0;
         monomial_row<double>(xs[2 * i], xs[2 * i + 1], deg, P + i * m, 1);
@@ -694,10 +714,17 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
         __syncwarp();
         RegRows<SP> RP;
         fill_phi_rows<SP>(RP, x32, n, p, lane);
-        bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
+        // the FP64 Phi passes ride along the first Gauss-Jordan steps
+        const int npass = (n * (n - 1) / 2 + 63) / 64;
+        bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane, [&](int c) {
+            if (RBFFD_SCHUR_INTERLEAVE && c < npass) phi_pair_pass(xs, n, p, phiP, 64 * c, lane);
+        });
         if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
         bool fallback = !ok;
-        if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, lane);
+        if (ok) {
+            const int done = RBFFD_SCHUR_INTERLEAVE ? (npass < 8 ? npass : 8) : 0;
+            assemble_phi_packed(xs, n, m, deg, p, phiP, P, done, lane);
+        }
         int64_t r0, r1;
         system_rows(a, sys, j, r0, r1);
         int iters_max = 0;

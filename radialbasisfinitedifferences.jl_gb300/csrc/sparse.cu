@@ -105,6 +105,43 @@ __global__ void __launch_bounds__(256) csr_to_sell_kernel(int64_t rows, int K, c
 // column-id load is a fully coalesced line, so no shared-memory staging is needed and the
 // kernel runs at full occupancy (the latency of the x gathers is hidden by warps, not
 // stages); each row accumulates in four independent FP64 chains.
+// Streamed read-only loads that the compiler may schedule freely (no volatile asm, so all of a
+// row's weight and column-id loads can be in flight together) with an L2 evict-first hint.
+#ifndef RBFFD_SELL_LOAD
+#define RBFFD_SELL_LOAD 2
+#endif
+#ifndef RBFFD_SELL_BATCH
+#define RBFFD_SELL_BATCH 10
+#endif
+__device__ __forceinline__ double ld_stream(const double *p, unsigned long long pol)
+{
+#if RBFFD_SELL_LOAD == 0
+    (void)pol;
+    return __ldcs(p);
+#elif RBFFD_SELL_LOAD == 1
+    (void)pol;
+    return __ldg(p);
+#else
+    double v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+#endif
+}
+__device__ __forceinline__ int ld_stream(const int32_t *p, unsigned long long pol)
+{
+#if RBFFD_SELL_LOAD == 0
+    (void)pol;
+    return __ldcs(p);
+#elif RBFFD_SELL_LOAD == 1
+    (void)pol;
+    return __ldg(p);
+#else
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+#endif
+}
+
 template <int K>
 __global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const int32_t *__restrict__ scol,
                                                      const double *__restrict__ sval, const double *__restrict__ x,
@@ -114,21 +151,45 @@ __global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const
     const int lane = threadIdx.x & 31;
     const int64_t ntile = (rows + 31) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; tile < ntile; tile += nw) {
         const int32_t *c = scol + tile * 32 * k + lane;
         const double *v = sval + tile * 32 * k + lane;
         double a[4] = {0.0, 0.0, 0.0, 0.0};
         if constexpr (K > 0) {
+#if RBFFD_SELL_BATCH > 0
+            constexpr int BT = RBFFD_SELL_BATCH;
 #pragma unroll
-            for (int t = 0; t < K; t++) a[t & 3] = fma(__ldcs(v + 32 * t), __ldg(x + __ldcs(c + 32 * t)), a[t & 3]);
+            for (int t0 = 0; t0 < K; t0 += BT) {
+                int cc[BT];
+                double vv[BT], xx[BT];
+#pragma unroll
+                for (int u = 0; u < BT; u++)
+                    if (t0 + u < K) {
+                        cc[u] = ld_stream(c + 32 * (t0 + u), pol);
+                        vv[u] = ld_stream(v + 32 * (t0 + u), pol);
+                    }
+#pragma unroll
+                for (int u = 0; u < BT; u++)
+                    if (t0 + u < K) xx[u] = __ldg(x + cc[u]);
+#pragma unroll
+                for (int u = 0; u < BT; u++)
+                    if (t0 + u < K) a[(t0 + u) & 3] = fma(vv[u], xx[u], a[(t0 + u) & 3]);
+            }
+#else
+#pragma unroll
+            for (int t = 0; t < K; t++)
+                a[t & 3] = fma(ld_stream(v + 32 * t, pol), __ldg(x + ld_stream(c + 32 * t, pol)), a[t & 3]);
+#endif
         } else {
             int t = 0;
             for (; t + 4 <= k; t += 4) {
 #pragma unroll
                 for (int u = 0; u < 4; u++)
-                    a[u] = fma(__ldcs(v + 32 * (t + u)), __ldg(x + __ldcs(c + 32 * (t + u))), a[u]);
+                    a[u] = fma(ld_stream(v + 32 * (t + u), pol), __ldg(x + ld_stream(c + 32 * (t + u), pol)), a[u]);
             }
-            for (; t < k; t++) a[0] = fma(__ldcs(v + 32 * t), __ldg(x + __ldcs(c + 32 * t)), a[0]);
+            for (; t < k; t++) a[0] = fma(ld_stream(v + 32 * t, pol), __ldg(x + ld_stream(c + 32 * t, pol)), a[0]);
         }
         const int64_t r = tile * 32 + lane;
         if (r < rows) __stcs(y + r, (a[0] + a[1]) + (a[2] + a[3]));
@@ -322,6 +383,136 @@ __global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int3
     }
 }
 
+// 16-byte vectors of fields: 4 floats or 2 doubles per lane.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using V = float4;
+    static constexpr int N = 4;
+    __device__ static V zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+    __device__ static V fma1(float a, V x, V y)
+    {
+        return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+    }
+    __device__ static V add(V a, V b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+};
+template <>
+struct Vec16<double> {
+    using V = double2;
+    static constexpr int N = 2;
+    __device__ static V zero() { return make_double2(0.0, 0.0); }
+    __device__ static V fma1(double a, V x, V y) { return make_double2(fma(a, x.x, y.x), fma(a, x.y, y.y)); }
+    __device__ static V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
+};
+
+// Sum over the row's entries of val[t] * x[col[t]][...] for this lane's 16-byte group of
+// fields: LPR = F / Vec16::N lanes share a row (a warp holds 32 / LPR rows), entries are
+// loaded once per LPR-wide round and broadcast inside the row's lane group by shuffles;
+// rows past their length (or past the end) contribute weight 0 from column 0.
+template <typename T>
+__device__ __forceinline__ typename Vec16<T>::V row_vec(int64_t a, int len, int lenmax, const int32_t *__restrict__ col,
+                                                       const T *__restrict__ val, const T *__restrict__ x, int F,
+                                                       int LPR, int sl)
+{
+    using VT = Vec16<T>;
+    typename VT::V s0 = VT::zero(), s1 = VT::zero();
+    const typename VT::V *xv = reinterpret_cast<const typename VT::V *>(x) + sl;
+    const int FV = F / VT::N;
+    for (int t0 = 0; t0 < lenmax; t0 += LPR) {
+        const int tl = t0 + sl;
+        int cl = 0;
+        T wl = 0;
+        if (tl < len) {
+            cl = __ldg(col + a + tl);
+            wl = __ldg(val + a + tl);
+        }
+        const int cnt = lenmax - t0 < LPR ? lenmax - t0 : LPR;
+        int t = 0;
+        for (; t + 2 <= cnt; t += 2) {
+            const int c0 = __shfl_sync(0xffffffffu, cl, t, LPR), c1 = __shfl_sync(0xffffffffu, cl, t + 1, LPR);
+            const T w0 = __shfl_sync(0xffffffffu, wl, t, LPR), w1 = __shfl_sync(0xffffffffu, wl, t + 1, LPR);
+            s0 = VT::fma1(w0, __ldg(xv + (int64_t)c0 * FV), s0);
+            s1 = VT::fma1(w1, __ldg(xv + (int64_t)c1 * FV), s1);
+        }
+        if (t < cnt) {
+            const int c0 = __shfl_sync(0xffffffffu, cl, t, LPR);
+            const T w0 = __shfl_sync(0xffffffffu, wl, t, LPR);
+            s0 = VT::fma1(w0, __ldg(xv + (int64_t)c0 * FV), s0);
+        }
+    }
+    return VT::add(s0, s1);
+}
+
+// RK4 stage (same modes as rk4_stage_kernel) with 16-byte field vectors: F / Vec16::N lanes
+// per row, 32 / that rows per warp, rows in Z-order chunks of 64 per CTA.  Needs F a multiple
+// of Vec16::N with F / Vec16::N dividing 32.
+template <typename T>
+__global__ void __launch_bounds__(256) rk4_stage_vec_kernel(int64_t rows, const int32_t *__restrict__ order,
+                                                            const int64_t *__restrict__ row_ptr,
+                                                            const int32_t *__restrict__ col, const T *__restrict__ val,
+                                                            const T *__restrict__ w, const T *__restrict__ u,
+                                                            T *__restrict__ acc, T *__restrict__ out,
+                                                            const uint8_t *__restrict__ fixed, int F, T c, int mode)
+{
+    using VT = Vec16<T>;
+    using V = typename VT::V;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int LPR = F / VT::N, RPW = 32 / LPR, sub = lane / LPR, sl = lane - sub * LPR;
+    const int64_t nchunk = (rows + 63) >> 6;
+    for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        for (int k = 0; k < 64; k += 8 * RPW) {
+            const int64_t idx = ch * 64 + k + wib * RPW + sub;
+            const bool valid = idx < rows;
+            const int64_t r = valid ? (order ? (int64_t)order[idx] : idx) : 0;
+            const int64_t a = valid ? row_ptr[r] : 0;
+            const bool fx = !valid || (fixed && fixed[r]);
+            const int len = fx ? 0 : (int)(row_ptr[r + 1] - a);
+            const int lenmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)len);
+            if (lenmax == 0 && !__any_sync(0xffffffffu, valid)) break;
+            V v = VT::zero();
+            if (lenmax > 0) v = row_vec<T>(a, len, lenmax, col, val, w, F, LPR, sl);
+            if (!valid) continue;
+            const int64_t o = r * (F / VT::N) + sl;
+            const V uu = reinterpret_cast<const V *>(u)[o];
+            V *po = reinterpret_cast<V *>(out) + o;
+            V *pa = reinterpret_cast<V *>(acc) + o;
+            if (mode == 0) {
+                *pa = v;
+                *po = VT::fma1(c, v, uu);
+            } else if (mode == 1) {
+                *pa = VT::fma1((T)2, v, *pa);
+                *po = VT::fma1(c, v, uu);
+            } else {
+                *po = VT::fma1(c, VT::add(*pa, v), uu);
+            }
+        }
+    }
+}
+
+// y = A x on F fields with 16-byte field vectors (rows in natural order).
+template <typename T>
+__global__ void __launch_bounds__(256) spmm_vec_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
+                                                       const int32_t *__restrict__ col, const T *__restrict__ val,
+                                                       const T *__restrict__ x, T *__restrict__ y, int F)
+{
+    using VT = Vec16<T>;
+    using V = typename VT::V;
+    const int lane = threadIdx.x & 31;
+    const int LPR = F / VT::N, RPW = 32 / LPR, sub = lane / LPR, sl = lane - sub * LPR;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r0 = warp * RPW; r0 < rows; r0 += nw * RPW) {
+        const int64_t r = r0 + sub;
+        const bool valid = r < rows;
+        const int64_t a = valid ? row_ptr[r] : 0;
+        const int len = valid ? (int)(row_ptr[r + 1] - a) : 0;
+        const int lenmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)len);
+        const V v = row_vec<T>(a, len, lenmax, col, val, x, F, LPR, sl);
+        if (valid) reinterpret_cast<V *>(y)[r * (F / VT::N) + sl] = v;
+    }
+}
+
 // val_out = sum_q coef[q] * val_q (operators with one sparsity pattern), in FP64 and FP32.
 __global__ void combine_ops_kernel(int64_t nnz, const double *const *vals, const double *coef, int nq,
                                    double *out64, float *out32)
@@ -458,6 +649,17 @@ int blocks_for(int64_t n, int threads, int64_t cap = 65535 * 4)
     return (int)b;
 }
 
+// The 16-byte field-vector kernels apply when F is a multiple of the vector width, the lanes
+// of a row (F / width) divide a warp, and every field array is 16-byte aligned.
+bool vec_fields_ok(int F, int dtype, const void *a, const void *b, const void *c, const void *d)
+{
+    const int vw = dtype == 0 ? 2 : 4;
+    if (F % vw) return false;
+    const int lpr = F / vw;
+    if (lpr > 32 || (32 % lpr)) return false;
+    return ((((uintptr_t)a) | ((uintptr_t)b) | ((uintptr_t)c) | ((uintptr_t)d)) & 15u) == 0;
+}
+
 // One CTA of up to 8 warps per SM, each warp with RBFFD_SPMV_STAGES K-row-tile stages.
 template <int K>
 cudaError_t launch_spmv_pipe(int64_t rows, const int32_t *col, const double *val, const double *x, double *y,
@@ -542,6 +744,17 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
 {
     if (rows <= 0) return cudaSuccess;
     int threads = 256;
+    if (vec_fields_ok(nfields, dtype, x, y, y, y)) {
+        const int rpw = 32 / (nfields / (dtype == 0 ? 2 : 4));
+        const int blocks = blocks_for((rows + rpw - 1) / rpw * 32, threads, 152 * 64);
+        if (dtype == 0)
+            spmm_vec_kernel<double><<<blocks, threads, 0, st>>>(rows, row_ptr, col, (const double *)val,
+                                                                (const double *)x, (double *)y, nfields);
+        else
+            spmm_vec_kernel<float><<<blocks, threads, 0, st>>>(rows, row_ptr, col, (const float *)val,
+                                                               (const float *)x, (float *)y, nfields);
+        return cudaGetLastError();
+    }
     int blocks = blocks_for(rows * 32, threads, 152 * 64);
     if (dtype == 0)
         spmm_kernel<double><<<blocks, threads, 0, st>>>(rows, row_ptr, col, (const double *)val,
@@ -558,6 +771,17 @@ cudaError_t launch_rk4_stage(int64_t rows, const int32_t *order, const int64_t *
 {
     if (rows <= 0) return cudaSuccess;
     int blocks = blocks_for((rows + 63) / 64, 1, (int64_t)num_sms * 8);
+    if (vec_fields_ok(F, dtype, w, u, acc, out)) {
+        if (dtype == 0)
+            rk4_stage_vec_kernel<double><<<blocks, 256, 0, st>>>(rows, order, row_ptr, col, (const double *)val,
+                                                                 (const double *)w, (const double *)u, (double *)acc,
+                                                                 (double *)out, fixed, F, c, mode);
+        else
+            rk4_stage_vec_kernel<float><<<blocks, 256, 0, st>>>(rows, order, row_ptr, col, (const float *)val,
+                                                                (const float *)w, (const float *)u, (float *)acc,
+                                                                (float *)out, fixed, F, (float)c, mode);
+        return cudaGetLastError();
+    }
     if (dtype == 0)
         rk4_stage_kernel<double><<<blocks, 256, 0, st>>>(rows, order, row_ptr, col, (const double *)val, (const double *)w,
                                                          (const double *)u, (double *)acc, (double *)out, fixed, F, c,

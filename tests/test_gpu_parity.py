@@ -303,10 +303,12 @@ def test_errors(pkg, gpu):
     assert np.allclose(E.toarray(), np.eye(len(X)), atol=1e-10)
 
 
+@pytest.mark.parametrize("F", [5, 64])
 @pytest.mark.parametrize("dtype,tol", [("f64", 1e-10), ("f32", 2e-5)])
-def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol):
+def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol, F):
     """RK4 of du/dt = L u, L = -Dx - 0.5 Dy + 0.01 Lap, boundary band held fixed, against a
-    numpy RK4 with the oracle's operators (7 steps: three graph-replayed pairs + one)."""
+    numpy RK4 with the oracle's operators (7 steps: three graph-replayed pairs + one).  F = 5
+    takes the lane-per-field kernels, F = 64 the 16-byte field-vector kernels."""
     import scipy.sparse as sp
     import torch
 
@@ -319,7 +321,6 @@ def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol):
     L = sum(c * sp.csr_matrix((ref["W"][q].ravel(), (rows, ref["cols"].ravel())), shape=(N, N))
             for q, c in enumerate(coef))
     fixed = ((X < 1.5 * h) | (X > 1 - 1.5 * h)).any(1)
-    F = 5
     U0 = np.random.default_rng(4).standard_normal((N, F))
     dt, nsteps = 0.1 * h, 7
 
