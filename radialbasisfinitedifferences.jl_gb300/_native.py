@@ -127,11 +127,12 @@ def load(build_if_missing=False):
     global _lib
     if _lib is not None:
         return _lib
-    if build_if_missing and not os.path.exists(_build.LIB_PATH):
+    path = os.environ.get("RBFFD_LIB") or _build.LIB_PATH  # RBFFD_LIB: another build of the library
+    if build_if_missing and not os.path.exists(path):
         _build.build()
-    if not os.path.exists(_build.LIB_PATH):
-        raise RuntimeError(f"librbffd.so not built ({_build.LIB_PATH}); run __graft_entry__.build()")
-    L = ctypes.CDLL(_build.LIB_PATH)
+    if not os.path.exists(path):
+        raise RuntimeError(f"librbffd.so not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
     P, i32, i64, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint32
     sig = {
         "rbffd_version": ([], i32),

@@ -38,9 +38,14 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 #ifndef RBFFD_SCHUR_MIN_BLOCKS
 #define RBFFD_SCHUR_MIN_BLOCKS 4
 #endif
-// 1: the FP64 Phi passes run inside the first Gauss-Jordan steps (see reg_gj's hook).
+// 1: for stencils of <= 32 nodes the FP64 Phi passes run inside the first Gauss-Jordan steps
+// (see reg_gj's hook; measured slower for the 64-row variant, so it is off there).
 #ifndef RBFFD_SCHUR_INTERLEAVE
 #define RBFFD_SCHUR_INTERLEAVE 1
+#endif
+// 1: residuals after the first are r - A d in double-float FP32 arithmetic (residual_df).
+#ifndef RBFFD_SCHUR_DF_RESIDUAL
+#define RBFFD_SCHUR_DF_RESIDUAL 1
 #endif
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
@@ -459,7 +464,8 @@ __device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
 // NE (1 or 2) elements (i, q) of r = b - A x for the Phi rows, elements e0 + lane + 32 u.
 template <int NE>
 __device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r,
-                                                  const double *B, const double *X, float *R32, int e0, int lane)
+                                                  double *B, const double *X, float *R32, int e0, bool store_r,
+                                                  int lane)
 {
     const int tot = n * r;
     int ee[NE], ii[NE], qq[NE], off[NE];
@@ -509,21 +515,25 @@ __device__ __forceinline__ void residual_phi_rows(const double *phiP, const doub
     }
 #pragma unroll
     for (int u = 0; u < NE; u++)
-        if (ee[u] < tot) R32[ee[u]] = f64_to_f32(a0[u] + a1[u]);
+        if (ee[u] < tot) {
+            const double v = a0[u] + a1[u];
+            if (store_r) B[ee[u]] = v;
+            R32[ee[u]] = f64_to_f32(v);
+        }
 }
 
-// R32 <- float(B - A X) with FP64 products, lane-per-element: ceil(n r / 32) lane-full passes
+// R32 <- float(B - A X) (and B <- B - A X when store_r) with FP64 products, lane-per-element: ceil(n r / 32) lane-full passes
 // of n + m FMAs for the Phi rows (two passes interleaved per lane), one pass of n FMAs per 32
 // elements for the P' rows.  Phi is read from its packed lower triangle.
 __device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r,
-                                              const double *B, const double *X, float *R32, int lane)
+                                              double *B, const double *X, float *R32, bool store_r, int lane)
 {
     const int tot = n * r;
     for (int e0 = 0; e0 < tot; e0 += 64) {
         if (e0 + 32 < tot)
-            residual_phi_rows<2>(phiP, P, n, m, r, B, X, R32, e0, lane);
+            residual_phi_rows<2>(phiP, P, n, m, r, B, X, R32, e0, store_r, lane);
         else
-            residual_phi_rows<1>(phiP, P, n, m, r, B, X, R32, e0, lane);
+            residual_phi_rows<1>(phiP, P, n, m, r, B, X, R32, e0, store_r, lane);
     }
     for (int e = lane; e < m * r; e += 32) {
         const int l = e / r, q = e - l * r;
@@ -534,7 +544,134 @@ __device__ __forceinline__ void residual_schur(const double *phiP, const double 
             a1 = fma(-P[(jj + 1) * m + l], X[(jj + 1) * r + q], a1);
         }
         if (jj < n) a0 = fma(-P[jj * m + l], X[jj * r + q], a0);
-        R32[(n + l) * r + q] = f64_to_f32(a0 + a1);
+        const double v = a0 + a1;
+        if (store_r) B[(n + l) * r + q] = v;
+        R32[(n + l) * r + q] = f64_to_f32(v);
+    }
+    __syncwarp();
+}
+
+// a = hi + lo with hi the float truncation of a and lo the float truncation of the remaining
+// 29 mantissa bits (|a - hi - lo| <= 2^-47 |a|), from the bit fields (integer pipe).
+__device__ __forceinline__ void split_f64(double a, float &hi, float &lo)
+{
+    hi = f64_to_f32(a);
+    const unsigned h = (unsigned)__double2hiint(a), l = (unsigned)__double2loint(a);
+    const int e = (int)((h >> 20) & 0x7ffu);
+    const unsigned rem = l & 0x1fffffffu;  // mantissa bits below the float's 23
+    // rem * 2^(e - 1075), exact in the integer-to-float conversion up to rounding of 29 -> 24 bits
+    const int ex = e - 1075 + 127;
+    const float scale = ex > 0 && ex < 255 ? __uint_as_float((unsigned)ex << 23) : 0.0f;
+    const float v = __uint2float_rz(rem) * scale;
+    lo = (h & 0x80000000u) ? -v : v;
+}
+
+// s_hi + s_lo += a * d for floats a, d: the product exactly (TwoProduct by FMA), the sum by
+// TwoSum into s_hi with every rounding error collected in s_lo (the double-float dot product
+// of Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 2005).
+__device__ __forceinline__ void df_mac(float a, float d, float &s_hi, float &s_lo)
+{
+    const float p = a * d;
+    const float e = fmaf(a, d, -p);
+    const float s = s_hi + p;
+    const float bb = s - s_hi;
+    const float err = (s_hi - (s - bb)) + (p - bb);
+    s_hi = s;
+    s_lo += err + e;
+}
+
+// Residual after a correction, r_new = r_old - A d, without FP64 products: d (the last
+// correction, R32) is a float vector, A = hi + lo splits exactly enough, A d is accumulated as
+// a double-float sum, and only r_old - (s_hi + s_lo) is formed in FP64 (two adds per element).
+// The error of A d is ~2^-44 |A||d| with |d| ~ 1e-5 |x|, far below FP64 rounding of |A||x|,
+// so the refinement converges as with an FP64 residual.  B holds r_old and receives r_new;
+// R32 receives float(r_new).  Phi rows lane-per-row (the split of Phi_ij shared by the row's
+// operators), P' rows lane-per-element.
+template <int SP, int SM, int RMAX>
+__device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, double *B,
+                                            float *R32, int lane)
+{
+    constexpr int NS = SP / 32;
+    float sh[NS][RMAX], sl[NS][RMAX];
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+#pragma unroll
+        for (int q = 0; q < RMAX; q++) sh[k][q] = sl[k][q] = 0.0f;
+        if (32 * k >= n) continue;
+        const int i = lane + 32 * k;
+        const int ii = i < n ? i : n - 1;
+        const int offi = tri_off(ii);
+        int offj = 0;
+        for (int jj = 0; jj < n; jj++) {
+            const int ad = jj <= ii ? offi + jj : offj + ii;
+            offj += jj + 1;
+            float ah, al;
+            split_f64(phiP[ad], ah, al);
+            const float *dj = R32 + jj * r;
+#pragma unroll
+            for (int q = 0; q < RMAX; q++) {
+                if (q < r) {
+                    const float d = dj[q];
+                    df_mac(ah, d, sh[k][q], sl[k][q]);
+                    sl[k][q] = fmaf(al, d, sl[k][q]);
+                }
+            }
+        }
+        for (int l = 0; l < m; l++) {
+            float ah, al;
+            split_f64(P[ii * m + l], ah, al);
+            const float *dl = R32 + (n + l) * r;
+#pragma unroll
+            for (int q = 0; q < RMAX; q++) {
+                if (q < r) {
+                    const float d = dl[q];
+                    df_mac(ah, d, sh[k][q], sl[k][q]);
+                    sl[k][q] = fmaf(al, d, sl[k][q]);
+                }
+            }
+        }
+    }
+    constexpr int PE = (SM * RMAX + 31) / 32;  // P' elements per lane (m r <= SM RMAX)
+    float th[PE], tl[PE];
+#pragma unroll
+    for (int u = 0; u < PE; u++) {
+        th[u] = tl[u] = 0.0f;
+        const int e = lane + 32 * u;
+        if (e < m * r) {
+            const int l = e / r, q = e - l * r;
+            for (int jj = 0; jj < n; jj++) {
+                float ah, al;
+                split_f64(P[jj * m + l], ah, al);
+                const float d = R32[jj * r + q];
+                df_mac(ah, d, th[u], tl[u]);
+                tl[u] = fmaf(al, d, tl[u]);
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        const int i = lane + 32 * k;
+        if (i < n) {
+#pragma unroll
+            for (int q = 0; q < RMAX; q++) {
+                if (q < r) {
+                    const double v = (B[i * r + q] - f32_to_f64(sh[k][q])) - f32_to_f64(sl[k][q]);
+                    B[i * r + q] = v;
+                    R32[i * r + q] = f64_to_f32(v);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < PE; u++) {
+        const int e = lane + 32 * u;
+        if (e < m * r) {
+            const int idx = n * r + e;
+            const double v = (B[idx] - f32_to_f64(th[u])) - f32_to_f64(tl[u]);
+            B[idx] = v;
+            R32[idx] = f64_to_f32(v);
+        }
     }
     __syncwarp();
 }
@@ -717,12 +854,12 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
         // the FP64 Phi passes ride along the first Gauss-Jordan steps
         const int npass = (n * (n - 1) / 2 + 63) / 64;
         bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane, [&](int c) {
-            if (RBFFD_SCHUR_INTERLEAVE && c < npass) phi_pair_pass(xs, n, p, phiP, 64 * c, lane);
+            if (RBFFD_SCHUR_INTERLEAVE && SP <= 32 && c < npass) phi_pair_pass(xs, n, p, phiP, 64 * c, lane);
         });
         if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
         bool fallback = !ok;
         if (ok) {
-            const int done = RBFFD_SCHUR_INTERLEAVE ? (npass < 8 ? npass : 8) : 0;
+            const int done = (RBFFD_SCHUR_INTERLEAVE && SP <= 32) ? (npass < 8 ? npass : 8) : 0;
             assemble_phi_packed(xs, n, m, deg, p, phiP, P, done, lane);
         }
         int64_t r0, r1;
@@ -740,8 +877,10 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                 if (it == 0) {
                     for (int e = lane; e < s * r; e += 32) R32[e] = f64_to_f32(B[e]);
                     __syncwarp();
+                } else if (it == 1 || !RBFFD_SCHUR_DF_RESIDUAL) {
+                    residual_schur(phiP, P, n, m, r, B, X, R32, RBFFD_SCHUR_DF_RESIDUAL != 0, lane);
                 } else {
-                    residual_schur(phiP, P, n, m, r, B, X, R32, lane);
+                    residual_df<SP, SM, RMAX>(phiP, P, n, m, r, B, R32, lane);
                 }
                 schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
                 unsigned dkey = 0u, xkey = 0u;
