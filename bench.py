@@ -53,6 +53,12 @@ def parse():
 
 WORKLOAD = dict(p=3, n=30, deg=3, ops=("Dx", "Dy", "Lap"))
 
+# DRAM traffic per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum):
+# the mixed solve on 512x512 nodes (262,144 systems; traffic is the gathered stencils and the
+# CSR output, so it scales with the systems) and the SELL SpMV on 1024x1024 nodes (31.46 M nnz).
+NCU_TRAFFIC = {"solve_bytes_per_system": (47.78e6 + 174.54e6) / 262144,
+               "spmv_bytes_per_nnz": (385.90e6 + 4.11e6) / 31457280}
+
 
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -450,7 +456,8 @@ def run_ours(args):
             "peak": fp64_peak.value,
             "unit": "TFLOP/s",
             "frac": solve_ach / fp64_peak.value if fp64_peak.value else None,
-            "traffic": None,
+            "traffic": NCU_TRAFFIC["solve_bytes_per_system"] * rows_per,
+            "traffic_note": "bytes per launch, ncu on 512x512 scaled by systems (stencil gathers + CSR output)",
             "note": "FP64 work of the mixed solve (A assembly, RHS, refinement residuals) over the kernel's "
                     "event-timed duration, against the measured FP64 FMA peak (rbffd_measure_fma_peaks)",
         },
@@ -461,7 +468,7 @@ def run_ours(args):
             "peak": hbm,
             "unit": "GB/s",
             "frac": spmv_gbs / hbm,
-            "traffic": None,
+            "traffic": NCU_TRAFFIC["spmv_bytes_per_nnz"] * nnz,
             "algorithmic_bytes": spmv_bytes,
             "peak_source": hbm_src,
         },

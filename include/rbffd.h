@@ -226,6 +226,27 @@ int rbffd_rk4_apply(rbffd_handle *h, rbffd_rk4 *rk, const void *x, void *y);
 void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk);
 
 /* ---------------------------------------------------------------------------------
+ * Least squares on an operator set: the assembly and solve of test/poisson_test.jl:75-121
+ * (`D[rows_b, :] .= c_b .* A_b[rows_b, :]`, row scaling, `D \ f`) on the GPU.  Row i of D is
+ * sum_q coef[q * rows + i] * A_q[i, :] over the set's operators (set order: E, Dx, Dy, Dxx, Dyy,
+ * Dxy, Lap, ...), and u minimises ||D u - f||_2, computed by CGLS (conjugate gradients on
+ * the normal equations, Hestenes-Stiefel form) with the set's CSR and CSC patterns; 50
+ * iterations run as one CUDA graph between convergence checks.  The reference solves with
+ * a sparse QR factorisation; CGLS reaches the same least-squares solution iteratively.
+ * ------------------------------------------------------------------------------ */
+typedef struct {
+    int64_t iterations; /* CGLS iterations done */
+    double relres;      /* ||D^T (f - D u)|| / ||D^T (f - D u0)|| at exit */
+    double ms;          /* device time of the iterations */
+} rbffd_lsq_info;
+
+/* coef: host, nops x rows (row-major by operator); f: host, rows; u: host, N (initial guess
+   in, solution out).  Stops when relres <= tol or after maxit iterations (relres is checked
+   every 50 iterations). */
+int rbffd_lsq_cgls(rbffd_handle *h, rbffd_opset *s, const double *coef, const double *f, double *u,
+                   int64_t maxit, double tol, rbffd_lsq_info *info);
+
+/* ---------------------------------------------------------------------------------
  * Allocation-free kNN (no counterpart in the reference).
  *
  * For callers that cannot allocate device memory: hosts whose device memory belongs to

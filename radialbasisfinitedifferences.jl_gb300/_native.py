@@ -40,6 +40,7 @@ EXPORTED = [
     "rbffd_rk4_run",
     "rbffd_rk4_apply",
     "rbffd_rk4_destroy",
+    "rbffd_lsq_cgls",
     "rbffd_knn_noalloc",
     "rbffd_measure_fma_peaks",
 ]
@@ -76,6 +77,10 @@ class Stats(ctypes.Structure):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "refine_hist"}
         d["refine_hist"] = list(self.refine_hist)
         return d
+
+
+class LsqInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("relres", ctypes.c_double), ("ms", ctypes.c_double)]
 
 
 class CSC(ctypes.Structure):
@@ -159,6 +164,7 @@ def load(build_if_missing=False):
         "rbffd_rk4_run": ([P, P, P, ctypes.c_double, i64], i32),
         "rbffd_rk4_apply": ([P, P, P, P], i32),
         "rbffd_rk4_destroy": ([P, P], None),
+        "rbffd_lsq_cgls": ([P, P, P, P, P, i64, ctypes.c_double, P], i32),
         "rbffd_knn_noalloc": ([P, i64, i32, P, P, P], i32),
         "rbffd_measure_fma_peaks": ([i32, P, P], i32),
     }

@@ -1207,6 +1207,105 @@ RBFFD_EXPORT void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk)
 }
 
 // ---------------------------------------------------------------------------
+// Least squares by CGLS on an operator set (test/poisson_test.jl:75-121).
+// ---------------------------------------------------------------------------
+namespace {
+cudaError_t cgls_iteration(rbffd_opset *s, const double *dD, const double *dDc, double *du, double *r, double *q,
+                           double *p, double *sv, double *part, double *sc, cudaStream_t st)
+{
+    cudaError_t e;
+    if ((e = launch_lsq_spmv(s->rows, s->row_ptr, s->col, dD, p, nullptr, q, part, st)) != cudaSuccess) return e;
+    if ((e = launch_lsq_final(part, sc, 1, 1, st)) != cudaSuccess) return e;
+    if ((e = launch_lsq_update_ur(s->N, s->rows, du, p, r, q, sc, st)) != cudaSuccess) return e;
+    if ((e = launch_lsq_spmv_t(s->N, s->csc_colptr, s->csc_rowval, s->row_begin, dDc, r, sv, part, st)) !=
+        cudaSuccess)
+        return e;
+    if ((e = launch_lsq_final(part, sc, 2, 0, st)) != cudaSuccess) return e;
+    return launch_lsq_update_p(s->N, p, sv, sc, 0, st);
+}
+}  // namespace
+
+RBFFD_EXPORT int rbffd_lsq_cgls(rbffd_handle *h, rbffd_opset *s, const double *coef, const double *f, double *u,
+                                int64_t maxit, double tol, rbffd_lsq_info *info)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || !coef || !f || !u || maxit < 0 || !(tol >= 0.0)) return fail(h, RBFFD_EINVAL, "bad lsq arguments");
+    cudaSetDevice(h->device);
+    int rc = ensure_csc(h, s);
+    if (rc) return rc;
+    cudaStream_t st = h->stream;
+    Arena tmp(st);
+    const int64_t rows = s->rows, cols = s->N, nnz = s->nnz;
+    double *dcoef, *dD, *dDc, *df, *du, *r, *q, *p, *sv, *part, *sc;
+    CK(tmp.get(&dcoef, (size_t)s->nops * rows));
+    CK(tmp.get(&dD, nnz));
+    CK(tmp.get(&dDc, nnz));
+    CK(tmp.get(&df, rows));
+    CK(tmp.get(&du, cols));
+    CK(tmp.get(&r, rows));
+    CK(tmp.get(&q, rows));
+    CK(tmp.get(&p, cols));
+    CK(tmp.get(&sv, cols));
+    CK(tmp.get(&part, lsq_partials()));
+    CK(tmp.zeros(&sc, 4));
+    CK(cudaMemcpyAsync(dcoef, coef, sizeof(double) * s->nops * rows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(df, f, sizeof(double) * rows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(du, u, sizeof(double) * cols, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(h->ev[0], st));
+    CK(launch_combine_rows(rows, s->row_ptr, s->val, nnz, s->nops, dcoef, dD, st));
+    CK(launch_gather_f64(nnz, s->csc_perm, dD, dDc, st));
+    // r = f - D u, s = D^T r, p = s, gamma0 = ||s||^2
+    CK(launch_lsq_spmv(rows, s->row_ptr, s->col, dD, du, df, r, part, st));
+    CK(launch_lsq_spmv_t(cols, s->csc_colptr, s->csc_rowval, s->row_begin, dDc, r, sv, part, st));
+    CK(launch_lsq_final(part, sc, 2, 0, st));
+    CK(launch_lsq_update_p(cols, p, sv, sc, 1, st));
+    CK(cudaMemcpyAsync(sc, sc + 2, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    double hsc[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(hsc, sc, sizeof(hsc), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double g0 = hsc[2];
+    double relres = g0 > 0.0 ? 1.0 : 0.0;
+    int64_t it = 0;
+    constexpr int CHUNK = 50;
+    cudaGraphExec_t gx = nullptr;
+    while (g0 > 0.0 && it < maxit && relres > tol) {
+        const int64_t n = maxit - it < CHUNK ? maxit - it : CHUNK;
+        if (n == CHUNK) {
+            if (!gx) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e1 = cudaSuccess;
+                for (int k = 0; k < CHUNK && e1 == cudaSuccess; k++)
+                    e1 = cgls_iteration(s, dD, dDc, du, r, q, p, sv, part, sc, st);
+                cudaError_t e2 = cudaStreamEndCapture(st, &g);
+                CK(e1);
+                CK(e2);
+                cudaError_t e3 = cudaGraphInstantiate(&gx, g, 0);
+                cudaGraphDestroy(g);
+                CK(e3);
+            }
+            CK(cudaGraphLaunch(gx, st));
+        } else {
+            for (int64_t k = 0; k < n; k++) CK(cgls_iteration(s, dD, dDc, du, r, q, p, sv, part, sc, st));
+        }
+        it += n;
+        CK(cudaMemcpyAsync(hsc, sc, sizeof(hsc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        relres = hsc[2] > 0.0 ? sqrt(hsc[2] / g0) : 0.0;
+    }
+    if (gx) cudaGraphExecDestroy(gx);
+    CK(cudaEventRecord(h->ev[1], st));
+    CK(cudaMemcpyAsync(u, du, sizeof(double) * cols, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (info) {
+        info->iterations = it;
+        info->relres = relres;
+        info->ms = elapsed(h->ev[0], h->ev[1]);
+    }
+    return RBFFD_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Drop-in entry points.
 // ---------------------------------------------------------------------------
 static int export_all(rbffd_handle *h, rbffd_opset *s, rbffd_csc *out)

@@ -157,6 +157,18 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
                         const void *val, const void *x, void *y, int nfields, int dtype,
                         cudaStream_t st);
 // RK4 stage (mode 0: first stage, 1: middle stages, 2: last stage), see sparse.cu.
+// CGLS building blocks (sparse.cu).
+int lsq_partials();
+cudaError_t launch_combine_rows(int64_t rows, const int64_t *row_ptr, const double *val, int64_t nnz, int nops,
+                                const double *coef, double *out, cudaStream_t st);
+cudaError_t launch_lsq_spmv(int64_t rows, const int64_t *row_ptr, const int32_t *col, const double *val,
+                            const double *x, const double *b, double *y, double *part, cudaStream_t st);
+cudaError_t launch_lsq_spmv_t(int64_t cols, const int64_t *colptr1, const int64_t *rowval1, int64_t row_begin,
+                              const double *vcsc, const double *x, double *y, double *part, cudaStream_t st);
+cudaError_t launch_lsq_final(const double *part, double *sc, int slot, int shift, cudaStream_t st);
+cudaError_t launch_lsq_update_ur(int64_t cols, int64_t rows, double *u, const double *p, double *r, const double *q,
+                                 const double *sc, cudaStream_t st);
+cudaError_t launch_lsq_update_p(int64_t cols, double *p, const double *s, const double *sc, int first, cudaStream_t st);
 // SELL-32 copy of a uniform-stencil operator set (all operators) and the SpMV on it.
 int64_t sell_padded(int64_t rows, int K);
 cudaError_t launch_csr_to_sell(int64_t rows, int K, const int32_t *col, const double *val, int nops, int64_t nnz,

@@ -513,6 +513,113 @@ __global__ void __launch_bounds__(256) spmm_vec_kernel(int64_t rows, const int64
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// CGLS for min ||D u - f|| (the least-squares solve of test/poisson_test.jl:115-119).
+// D is an operator set's sparsity pattern with row-wise combined values; D^T products use
+// the set's CSC permutation.  Scalars stay on the device: sc[0] = gamma (= ||D^T r||^2 of the
+// last iteration), sc[1] = ||D p||^2, sc[2] = the new gamma.  Reductions are deterministic
+// (fixed grid, per-block partials summed by one block in a fixed order).
+constexpr int LSQ_BLOCKS = 256;
+
+// D[t] = sum_q coef[q * rows + row(t)] * val[q * nnz + t] (thread per row)
+__global__ void combine_rows_kernel(int64_t rows, const int64_t *__restrict__ row_ptr, const double *__restrict__ val,
+                                    int64_t nnz, int nops, const double *__restrict__ coef, double *__restrict__ out)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t t = row_ptr[r]; t < row_ptr[r + 1]; t++) {
+            double v = 0.0;
+            for (int q = 0; q < nops; q++) v = fma(coef[(int64_t)q * rows + r], val[(int64_t)q * nnz + t], v);
+            out[t] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void block_sum_to(double v, double *part)
+{
+    __shared__ double red[32];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) part[blockIdx.x] = v;
+    }
+}
+
+// y = D x (thread per row) and per-block partial sums of y^2; with b != null, y = b - D x.
+__global__ void __launch_bounds__(256) lsq_spmv_kernel(int64_t rows, const int64_t *__restrict__ row_ptr,
+                                                       const int32_t *__restrict__ col, const double *__restrict__ val,
+                                                       const double *__restrict__ x, const double *__restrict__ b,
+                                                       double *__restrict__ y, double *__restrict__ part)
+{
+    double acc2 = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        for (int64_t t = row_ptr[r]; t < row_ptr[r + 1]; t++) v = fma(val[t], x[col[t]], v);
+        if (b) v = b[r] - v;
+        y[r] = v;
+        acc2 = fma(v, v, acc2);
+    }
+    block_sum_to(acc2, part);
+}
+
+// y = D^T x through the CSC (1-based colptr/rowval as exported to Julia, values vcsc in CSC
+// order), thread per column, and per-block partial sums of y^2.
+__global__ void __launch_bounds__(256) lsq_spmv_t_kernel(int64_t cols, const int64_t *__restrict__ colptr1,
+                                                         const int64_t *__restrict__ rowval1, int64_t row_begin,
+                                                         const double *__restrict__ vcsc, const double *__restrict__ x,
+                                                         double *__restrict__ y, double *__restrict__ part)
+{
+    double acc2 = 0.0;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        for (int64_t k = colptr1[j] - 1; k < colptr1[j + 1] - 1; k++) v = fma(vcsc[k], x[rowval1[k] - 1 - row_begin], v);
+        y[j] = v;
+        acc2 = fma(v, v, acc2);
+    }
+    block_sum_to(acc2, part);
+}
+
+// sc[slot] = sum of the partials (one block, fixed order); with shift, first sc[0] = sc[2].
+__global__ void lsq_final_kernel(const double *__restrict__ part, double *__restrict__ sc, int slot, int shift)
+{
+    double v = 0.0;
+    for (int i = threadIdx.x; i < LSQ_BLOCKS; i += blockDim.x) v += part[i];
+    __shared__ double red[32];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        if (shift) sc[0] = sc[2];
+        sc[slot] = t;
+    }
+}
+
+// u += alpha p (cols), r -= alpha q (rows), alpha = gamma / ||q||^2
+__global__ void lsq_update_ur(int64_t cols, int64_t rows, double *__restrict__ u, const double *__restrict__ p,
+                              double *__restrict__ r, const double *__restrict__ q, const double *__restrict__ sc)
+{
+    const double alpha = sc[1] > 0.0 ? sc[0] / sc[1] : 0.0;
+    const int64_t n = cols > rows ? cols : rows;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < cols) u[i] = fma(alpha, p[i], u[i]);
+        if (i < rows) r[i] = fma(-alpha, q[i], r[i]);
+    }
+}
+
+// p = s + beta p, beta = gamma_new / gamma (p = s on the first call: first != 0)
+__global__ void lsq_update_p(int64_t cols, double *__restrict__ p, const double *__restrict__ s,
+                             const double *__restrict__ sc, int first)
+{
+    const double beta = (!first && sc[0] > 0.0) ? sc[2] / sc[0] : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cols; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fma(beta, p[i], s[i]);
+}
+
 // val_out = sum_q coef[q] * val_q (operators with one sparsity pattern), in FP64 and FP32.
 __global__ void combine_ops_kernel(int64_t nnz, const double *const *vals, const double *coef, int nq,
                                    double *out64, float *out32)
@@ -738,6 +845,50 @@ cudaError_t launch_spmv_sell(int64_t rows, int K, const int32_t *scol, const dou
         spmv_f64_sell<0><<<blocks, 256, 0, st>>>(rows, K, scol, sval, x, y);
     return cudaGetLastError();
 }
+
+cudaError_t launch_combine_rows(int64_t rows, const int64_t *row_ptr, const double *val, int64_t nnz, int nops,
+                                const double *coef, double *out, cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    combine_rows_kernel<<<blocks_for(rows, 256), 256, 0, st>>>(rows, row_ptr, val, nnz, nops, coef, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsq_spmv(int64_t rows, const int64_t *row_ptr, const int32_t *col, const double *val,
+                            const double *x, const double *b, double *y, double *part, cudaStream_t st)
+{
+    lsq_spmv_kernel<<<LSQ_BLOCKS, 256, 0, st>>>(rows, row_ptr, col, val, x, b, y, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsq_spmv_t(int64_t cols, const int64_t *colptr1, const int64_t *rowval1, int64_t row_begin,
+                              const double *vcsc, const double *x, double *y, double *part, cudaStream_t st)
+{
+    lsq_spmv_t_kernel<<<LSQ_BLOCKS, 256, 0, st>>>(cols, colptr1, rowval1, row_begin, vcsc, x, y, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsq_final(const double *part, double *sc, int slot, int shift, cudaStream_t st)
+{
+    lsq_final_kernel<<<1, 256, 0, st>>>(part, sc, slot, shift);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsq_update_ur(int64_t cols, int64_t rows, double *u, const double *p, double *r, const double *q,
+                                 const double *sc, cudaStream_t st)
+{
+    const int64_t n = cols > rows ? cols : rows;
+    lsq_update_ur<<<blocks_for(n, 256), 256, 0, st>>>(cols, rows, u, p, r, q, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsq_update_p(int64_t cols, double *p, const double *s, const double *sc, int first, cudaStream_t st)
+{
+    lsq_update_p<<<blocks_for(cols, 256), 256, 0, st>>>(cols, p, s, sc, first);
+    return cudaGetLastError();
+}
+
+int lsq_partials() { return LSQ_BLOCKS; }
 
 cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
                         const void *x, void *y, int nfields, int dtype, cudaStream_t st)

@@ -407,6 +407,20 @@ class OperatorSet:
         self.h.synchronize()
         return y
 
+    def lsq_cgls(self, coef, f, u0=None, maxit=20000, tol=1e-12):
+        """u minimising ||D u - f|| with D[i, :] = sum_q coef[q, i] A_q[i, :] (operators in set
+        order), by CGLS on the GPU (rbffd_lsq_cgls): the `D \\ f` of test/poisson_test.jl.
+        Returns (u, iterations, relres)."""
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        if c.shape != (len(self.ops), self.rows):
+            raise ValueError("coef must be (number of operators, rows)")
+        fv = np.ascontiguousarray(f, dtype=np.float64)
+        u = np.zeros(self.cols) if u0 is None else np.array(u0, dtype=np.float64)
+        info = nat.LsqInfo()
+        nat.check(self.h.ptr, self._lib.rbffd_lsq_cgls(self.h.ptr, self.ptr, _ptr(c), _ptr(fv), _ptr(u), int(maxit),
+                                                       float(tol), ctypes.byref(info)))
+        return u, info.iterations, info.relres
+
     def close(self):
         if getattr(self, "ptr", None):
             self._lib.rbffd_opset_destroy(self.h.ptr, self.ptr)

@@ -177,6 +177,42 @@ def poisson_error(X, Y, E, Dx, Dy, Dxx, Dyy, t, orc):
     return np.linalg.norm(uY - ue(x, y)) / np.linalg.norm(ue(x, y))
 
 
+def test_poisson_reference_test_gpu_least_squares(pkg, orc, gpu, tominec):
+    """test/poisson_test.jl end to end on the GPU: operators, row assembly and scaling of D, and
+    the least-squares solve (CGLS, rbffd_lsq_cgls) -- same error as the dense solution."""
+    t = tominec
+    X = t["x_nodes"]
+    Y = t["y_nodes"].copy()
+    idx, _ = orc.knn(Y, X, 1)
+    Y[idx[:, 0]] = X
+    M, N = len(Y), len(X)
+    ii, idr, ine = t["y_idx_in"] - 1, t["y_idx_dirichlet"] - 1, t["y_idx_neumann"] - 1
+    nx, ny = t["x_normals"][:, 2], t["y_normals"][:, 2]
+    x, y = Y[:, 0], Y[:, 1]
+    ue = np.sin(2 * np.pi * x * y)
+    f = np.zeros(M)
+    f[ii] = x[ii] ** 2 * np.pi**2 * np.sin(x[ii] * y[ii] * np.pi * 2.0) * (-4.0) - y[ii] ** 2 * np.pi**2 * np.sin(
+        x[ii] * y[ii] * np.pi * 2.0) * 4.0
+    f[ine] = ny * x[ine] * np.pi * np.cos(x[ine] * y[ine] * np.pi * 2.0) * 2.0 + nx * y[ine] * np.pi * np.cos(
+        x[ine] * y[ine] * np.pi * 2.0) * 2.0
+    f[idr] = ue[idr]
+    _, d2 = orc.knn(X, X, 2)
+    h = np.mean(np.sqrt(d2[:, 1]))
+    sc = np.ones(M)
+    sc[ii], sc[ine], sc[idr] = 1 / np.sqrt(len(ii)), 1 / np.sqrt(len(ine)), 1 / h / np.sqrt(len(idr))
+    with pkg.OperatorSet(X, Y, 3, 20, 3, ops=("E", "Dx", "Dy", "Dxx", "Dyy")) as s:
+        coef = np.zeros((5, M))
+        coef[0, idr] = 1.0
+        coef[1, ine], coef[2, ine] = nx, ny
+        coef[3, ii] = coef[4, ii] = 1.0
+        u, iters, relres = s.lsq_cgls(coef * sc, f * sc, maxit=20000, tol=1e-13)
+        assert relres <= 1e-13, (iters, relres)
+        uY = s.csr("E") @ u
+    err = np.linalg.norm(uY - ue) / np.linalg.norm(ue)
+    assert err < 0.0027, err
+    assert abs(err - 0.0026578775) < 1e-8, err
+
+
 def test_hyperviscosity_reference_test(pkg, gpu, tominec):
     """test/hyperviscosity_test.jl: p=5, deg 5, n=42 on Tominec's nodes: Dxk ~ Dxx, Dyk ~ Dyy."""
     X = tominec["x_nodes"]
