@@ -39,9 +39,9 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 #define RBFFD_SCHUR_MIN_BLOCKS 4
 #endif
 // 1: for stencils of <= 32 nodes the FP64 Phi passes run inside the first Gauss-Jordan steps
-// (see reg_gj's hook; measured slower for the 64-row variant, so it is off there).
+// (reg_gj's hook).  Off by default: +1 % on uniform k = 30 batches, -8 % on mixed-size ones.
 #ifndef RBFFD_SCHUR_INTERLEAVE
-#define RBFFD_SCHUR_INTERLEAVE 1
+#define RBFFD_SCHUR_INTERLEAVE 0
 #endif
 // 1: residuals after the first are r - A d in double-float FP32 arithmetic (residual_df).
 #ifndef RBFFD_SCHUR_DF_RESIDUAL
