@@ -226,6 +226,29 @@ int rbffd_rk4_apply(rbffd_handle *h, rbffd_rk4 *rk, const void *x, void *y);
 void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk);
 
 /* ---------------------------------------------------------------------------------
+ * Ghost-node closure (examples/adv_diff_test.jl:108-141, 160-176).  For a boundary with
+ * boundary nodes B and ghost nodes G (|B| = |G|: one ghost per boundary node,
+ * src/genghostnodes.jl) and an operator A of a collocated set (Dx for the left/right, Dy for
+ * the top/bottom boundary in the example), the ghost values for which A u = 0 on B are
+ *     u[G] = -inv(A[B, G]) * (A[B, not G] * u[not G]).
+ * ------------------------------------------------------------------------------ */
+typedef struct rbffd_ghost rbffd_ghost;
+
+/* bnodes, gnodes: host, nb 0-based node ids each.  inv(A[B, G]) is formed once, on the GPU
+   (dense Gauss-Jordan with partial pivoting: the reference's inv(Array(w_bc_g))); a
+   singular block returns RBFFD_ESINGULAR.  The closure reads the set's operator, so the set
+   must outlive it. */
+int rbffd_ghost_create(rbffd_handle *h, rbffd_opset *s, int op, const int32_t *bnodes,
+                       const int32_t *gnodes, int64_t nb, rbffd_ghost **out);
+/* Overwrite u[G] (device fields [rows][nfields], dtype 0: FP64, 1: FP32) in place. */
+int rbffd_ghost_apply(rbffd_handle *h, rbffd_ghost *g, void *u, int nfields, int dtype);
+void rbffd_ghost_destroy(rbffd_handle *h, rbffd_ghost *g);
+/* Apply the closures (in order) to the input of every RK4 stage before L is applied; the
+   first stage's input is the state itself, which is overwritten as the reference's cons_sys
+   overwrites u.  ng = 0 removes them.  The closures must outlive the stepper's use. */
+int rbffd_rk4_set_closure(rbffd_handle *h, rbffd_rk4 *rk, rbffd_ghost *const *g, int ng);
+
+/* ---------------------------------------------------------------------------------
  * Least squares on an operator set: the assembly and solve of test/poisson_test.jl:75-121
  * (`D[rows_b, :] .= c_b .* A_b[rows_b, :]`, row scaling, `D \ f`) on the GPU.  Row i of D is
  * sum_q coef[q * rows + i] * A_q[i, :] over the set's operators (set order: E, Dx, Dy, Dxx, Dyy,

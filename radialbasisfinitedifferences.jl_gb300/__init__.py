@@ -8,6 +8,7 @@ the Julia host side.
 from . import _build, _native, nodesets  # noqa: F401
 from ._native import RbffdError  # noqa: F401
 from .operators import (  # noqa: F401
+    GhostClosure,
     RK4Stepper,
     GENERATE_OPS,
     HYPERVISCOSITY_OPS,

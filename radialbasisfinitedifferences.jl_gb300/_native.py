@@ -40,6 +40,10 @@ EXPORTED = [
     "rbffd_rk4_run",
     "rbffd_rk4_apply",
     "rbffd_rk4_destroy",
+    "rbffd_ghost_create",
+    "rbffd_ghost_apply",
+    "rbffd_ghost_destroy",
+    "rbffd_rk4_set_closure",
     "rbffd_lsq_cgls",
     "rbffd_knn_noalloc",
     "rbffd_measure_fma_peaks",
@@ -164,6 +168,10 @@ def load(build_if_missing=False):
         "rbffd_rk4_run": ([P, P, P, ctypes.c_double, i64], i32),
         "rbffd_rk4_apply": ([P, P, P, P], i32),
         "rbffd_rk4_destroy": ([P, P], None),
+        "rbffd_ghost_create": ([P, P, i32, P, P, i64, P], i32),
+        "rbffd_ghost_apply": ([P, P, P, i32, i32], i32),
+        "rbffd_ghost_destroy": ([P, P], None),
+        "rbffd_rk4_set_closure": ([P, P, P, i32], i32),
         "rbffd_lsq_cgls": ([P, P, P, P, P, i64, ctypes.c_double, P], i32),
         "rbffd_knn_noalloc": ([P, i64, i32, P, P, P], i32),
         "rbffd_measure_fma_peaks": ([i32, P, P], i32),

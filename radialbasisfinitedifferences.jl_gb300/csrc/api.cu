@@ -1007,6 +1007,18 @@ RBFFD_EXPORT int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void 
 // ---------------------------------------------------------------------------
 // RK4 time stepping on device-resident operators.
 // ---------------------------------------------------------------------------
+struct rbffd_ghost {
+    int64_t N = 0, nb = 0;
+    const int64_t *row_ptr = nullptr;  // the operator's CSR (owned by its set)
+    const int32_t *col = nullptr;
+    const double *val = nullptr;
+    int32_t *bnodes = nullptr, *gnodes = nullptr, *gidx = nullptr;
+    double *M = nullptr;  // [I | inv(A[B, G])] after the reduction, nb x 2nb
+    double *y = nullptr;  // nb x ycap scratch
+    int ycap = 0;
+    std::vector<void *> owned;
+};
+
 struct rbffd_rk4 {
     int64_t rows = 0, nnz = 0;
     int F = 0, dtype = 0;
@@ -1016,6 +1028,7 @@ struct rbffd_rk4 {
     float *val32 = nullptr;
     uint8_t *fixed = nullptr;
     int32_t *order = nullptr;  // rows in Morton (Z-curve) order of their nodes
+    std::vector<rbffd_ghost *> closures;  // applied to every stage input, in order
     void *unext = nullptr, *wA = nullptr, *wB = nullptr, *acc = nullptr;
     cudaGraphExec_t graph2 = nullptr;  // two steps u -> unext -> u
     const void *graph_u = nullptr;
@@ -1025,21 +1038,35 @@ struct rbffd_rk4 {
 
 namespace {
 // Enqueue one RK4 step u -> out on stream st.
-cudaError_t rk4_enqueue_step(rbffd_handle *h, rbffd_rk4 *rk, const void *u, void *out, double dt, cudaStream_t st)
+cudaError_t rk4_closures(rbffd_rk4 *rk, void *w, cudaStream_t st)
+{
+    for (rbffd_ghost *g : rk->closures) {
+        cudaError_t e = ghost_apply(g->nb, g->bnodes, g->gnodes, g->row_ptr, g->col, g->val, g->gidx, g->M, w, rk->F,
+                                    rk->dtype, g->y, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Enqueue one RK4 step u -> out on stream st; the ghost closures are applied to every stage
+// input first (u itself for the first stage, as the reference's cons_sys overwrites u).
+cudaError_t rk4_enqueue_step(rbffd_handle *h, rbffd_rk4 *rk, void *u, void *out, double dt, cudaStream_t st)
 {
     const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
-    cudaError_t e;
-    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, u, u, rk->acc, rk->wA, rk->fixed, rk->F, 0.5 * dt, 0,
-                         rk->dtype, h->num_sms, st);
-    if (e != cudaSuccess) return e;
-    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, rk->wB, rk->fixed, rk->F, 0.5 * dt,
-                         1, rk->dtype, h->num_sms, st);
-    if (e != cudaSuccess) return e;
-    e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wB, u, rk->acc, rk->wA, rk->fixed, rk->F, dt, 1,
-                         rk->dtype, h->num_sms, st);
-    if (e != cudaSuccess) return e;
-    return launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, rk->wA, u, rk->acc, out, rk->fixed, rk->F, dt / 6.0,
-                            2, rk->dtype, h->num_sms, st);
+    struct Stage {
+        void *w, *o;
+        double c;
+        int mode;
+    } stages[4] = {{u, rk->wA, 0.5 * dt, 0}, {rk->wA, rk->wB, 0.5 * dt, 1}, {rk->wB, rk->wA, dt, 1},
+                   {rk->wA, out, dt / 6.0, 2}};
+    for (const Stage &sg : stages) {
+        cudaError_t e = rk4_closures(rk, sg.w, st);
+        if (e != cudaSuccess) return e;
+        e = launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, sg.w, u, rk->acc, sg.o, rk->fixed, rk->F,
+                             sg.c, sg.mode, rk->dtype, h->num_sms, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 }  // namespace
 
@@ -1204,6 +1231,119 @@ RBFFD_EXPORT void rbffd_rk4_destroy(rbffd_handle *h, rbffd_rk4 *rk)
         cudaStreamSynchronize(h->stream);
     }
     delete rk;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost-node closure (examples/adv_diff_test.jl:108-141, 160-176).
+// ---------------------------------------------------------------------------
+RBFFD_EXPORT int rbffd_ghost_create(rbffd_handle *h, rbffd_opset *s, int op, const int32_t *bnodes,
+                                    const int32_t *gnodes, int64_t nb, rbffd_ghost **out)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!s || !bnodes || !gnodes || !out || nb <= 0 || op < 0 || op >= s->nops)
+        return fail(h, RBFFD_EINVAL, "bad ghost arguments");
+    *out = nullptr;
+    if (!s->collocated || s->row_begin != 0 || s->rows != s->N)
+        return fail(h, RBFFD_EINVAL, "the ghost closure needs a collocated full operator set");
+    if (nb > 46340) return fail(h, RBFFD_EINVAL, "more than 46340 ghost nodes in one boundary");
+    std::vector<char> seen(s->N, 0);
+    for (int64_t i = 0; i < nb; i++) {
+        if (bnodes[i] < 0 || bnodes[i] >= s->N || gnodes[i] < 0 || gnodes[i] >= s->N)
+            return fail(h, RBFFD_EINVAL, "ghost or boundary node out of range");
+        if (seen[gnodes[i]]++) return fail(h, RBFFD_EINVAL, "repeated ghost node");
+    }
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    Arena keep(st), tmp(st);
+    rbffd_ghost *g = new rbffd_ghost();
+    auto bail = [&](int code) {
+        delete g;
+        return code;
+    };
+    g->N = s->N;
+    g->nb = nb;
+    g->row_ptr = s->row_ptr;
+    g->col = s->col;
+    g->val = s->val + (size_t)op * s->nnz;
+    cudaError_t e = cudaSuccess;
+#define CKG(expr)                                                                                            \
+    do {                                                                                                     \
+        e = (expr);                                                                                          \
+        if (e != cudaSuccess) return bail(fail(h, RBFFD_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e))); \
+    } while (0)
+    double *fcol;
+    int *flag;
+    CKG(keep.get(&g->bnodes, nb));
+    CKG(keep.get(&g->gnodes, nb));
+    CKG(keep.get(&g->gidx, s->N));
+    CKG(keep.get(&g->M, (size_t)nb * 2 * nb));
+    CKG(tmp.get(&fcol, nb));
+    CKG(tmp.zeros(&flag, 1));
+    CKG(cudaMemcpyAsync(g->bnodes, bnodes, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, st));
+    CKG(cudaMemcpyAsync(g->gnodes, gnodes, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, st));
+    CKG(ghost_build(s->N, nb, g->bnodes, g->gnodes, g->row_ptr, g->col, g->val, g->gidx, g->M, fcol, flag, st));
+    int hflag = 0;
+    CKG(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CKG(cudaStreamSynchronize(st));
+#undef CKG
+    if (hflag) return bail(fail(h, RBFFD_ESINGULAR, "singular ghost block A[B, G]"));
+    keep.release_to(g->owned);
+    *out = g;
+    return RBFFD_OK;
+}
+
+static cudaError_t ghost_scratch(rbffd_handle *h, rbffd_ghost *g, int F)
+{
+    if (g->ycap >= F) return cudaSuccess;
+    double *y;
+    cudaError_t e = cudaMallocAsync((void **)&y, sizeof(double) * g->nb * F, h->stream);
+    if (e != cudaSuccess) return e;
+    g->owned.push_back(y);
+    g->y = y;
+    g->ycap = F;
+    return cudaSuccess;
+}
+
+RBFFD_EXPORT int rbffd_ghost_apply(rbffd_handle *h, rbffd_ghost *g, void *u, int nfields, int dtype)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!g || !u || nfields <= 0 || (dtype != 0 && dtype != 1)) return fail(h, RBFFD_EINVAL, "bad ghost_apply arguments");
+    cudaSetDevice(h->device);
+    CK(ghost_scratch(h, g, nfields));
+    CK(ghost_apply(g->nb, g->bnodes, g->gnodes, g->row_ptr, g->col, g->val, g->gidx, g->M, u, nfields, dtype, g->y,
+                   h->stream));
+    return RBFFD_OK;
+}
+
+RBFFD_EXPORT void rbffd_ghost_destroy(rbffd_handle *h, rbffd_ghost *g)
+{
+    if (!g) return;
+    if (h) {
+        cudaSetDevice(h->device);
+        for (void *p : g->owned) cudaFreeAsync(p, h->stream);
+        cudaStreamSynchronize(h->stream);
+    }
+    delete g;
+}
+
+RBFFD_EXPORT int rbffd_rk4_set_closure(rbffd_handle *h, rbffd_rk4 *rk, rbffd_ghost *const *g, int ng)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!rk || ng < 0 || (ng > 0 && !g)) return fail(h, RBFFD_EINVAL, "bad closure arguments");
+    cudaSetDevice(h->device);
+    std::vector<rbffd_ghost *> list;
+    for (int i = 0; i < ng; i++) {
+        if (!g[i] || g[i]->N != rk->rows) return fail(h, RBFFD_EINVAL, "closure of another node set");
+        CK(ghost_scratch(h, g[i], rk->F));
+        list.push_back(g[i]);
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    rk->closures = list;
+    if (rk->graph2) {  // the captured steps no longer match
+        cudaGraphExecDestroy(rk->graph2);
+        rk->graph2 = nullptr;
+    }
+    return RBFFD_OK;
 }
 
 // ---------------------------------------------------------------------------

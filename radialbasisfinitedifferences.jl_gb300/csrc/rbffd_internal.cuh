@@ -73,6 +73,47 @@ struct GridDev {
     const int32_t *cls;    // node classes in cell order (nullable)
 };
 
+// Conversions between float and double on the integer pipe (bit-field arithmetic; GB300
+// runs FP64 conversions on its 1/64-rate FP64 pipe).
+namespace {
+// float -> double from the IEEE-754 bit fields (exact for normal numbers; subnormals flush to
+// a signed zero; inf and NaN are kept).
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    unsigned u = __float_as_uint(f);
+    unsigned e = (u >> 23) & 0xffu;
+    unsigned sign = u & 0x80000000u;
+    unsigned mant = u & 0x7fffffu;
+    unsigned e64 = e == 255u ? 2047u : e + (1023u - 127u);
+    unsigned hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
+    unsigned lo = e == 0u ? 0u : (mant << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float by truncation of the mantissa (|error| < 1 ulp of float), from the bit
+// fields.  Magnitudes above the float range give inf, below the normal range a signed zero;
+// NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32(double d)
+{
+    unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    unsigned sign = hi & 0x80000000u;
+    int e = (int)((hi >> 20) & 0x7ffu);
+    int e32 = e - 1023 + 127;
+    unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned out;
+    if (e == 2047)
+        out = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
+    else if (e32 >= 255)
+        out = sign | 0x7f800000u;
+    else if (e32 <= 0)
+        out = sign;
+    else
+        out = sign | ((unsigned)e32 << 23) | mant;
+    return __uint_as_float(out);
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // Launch wrappers implemented in the .cu files.  All run on `st` and return a
 // cudaError_t of the launch; device-side failures are reported through flag words.
@@ -157,6 +198,13 @@ cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col
                         const void *val, const void *x, void *y, int nfields, int dtype,
                         cudaStream_t st);
 // RK4 stage (mode 0: first stage, 1: middle stages, 2: last stage), see sparse.cu.
+// Ghost-node closure building blocks (sparse.cu).
+cudaError_t ghost_build(int64_t N, int64_t nb, const int32_t *bnodes, const int32_t *gnodes, const int64_t *row_ptr,
+                        const int32_t *col, const double *val, int32_t *gidx, double *M, double *fcol, int *flag,
+                        cudaStream_t st);
+cudaError_t ghost_apply(int64_t nb, const int32_t *bnodes, const int32_t *gnodes, const int64_t *row_ptr,
+                        const int32_t *col, const double *val, const int32_t *gidx, const double *M, void *u, int F,
+                        int dtype, double *y, cudaStream_t st);
 // CGLS building blocks (sparse.cu).
 int lsq_partials();
 cudaError_t launch_combine_rows(int64_t rows, const int64_t *row_ptr, const double *val, int64_t nnz, int nops,

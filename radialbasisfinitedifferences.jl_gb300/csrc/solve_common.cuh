@@ -91,42 +91,6 @@ __device__ __forceinline__ float warp_max_f(float v)
 
 __device__ __forceinline__ bool is_zero64(double x) { return abs_key(x) == 0ull; }
 
-// float -> double from the IEEE-754 bit fields (exact for normal numbers; subnormals flush to
-// a signed zero; inf and NaN are kept).
-__device__ __forceinline__ double f32_to_f64(float f)
-{
-    unsigned u = __float_as_uint(f);
-    unsigned e = (u >> 23) & 0xffu;
-    unsigned sign = u & 0x80000000u;
-    unsigned mant = u & 0x7fffffu;
-    unsigned e64 = e == 255u ? 2047u : e + (1023u - 127u);
-    unsigned hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
-    unsigned lo = e == 0u ? 0u : (mant << 29);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
-// double -> float by truncation of the mantissa (|error| < 1 ulp of float), from the bit
-// fields.  Magnitudes above the float range give inf, below the normal range a signed zero;
-// NaN stays NaN.
-__device__ __forceinline__ float f64_to_f32(double d)
-{
-    unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    unsigned sign = hi & 0x80000000u;
-    int e = (int)((hi >> 20) & 0x7ffu);
-    int e32 = e - 1023 + 127;
-    unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    unsigned out;
-    if (e == 2047)
-        out = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
-    else if (e32 >= 255)
-        out = sign | 0x7f800000u;
-    else if (e32 <= 0)
-        out = sign;
-    else
-        out = sign | ((unsigned)e32 << 23) | mant;
-    return __uint_as_float(out);
-}
-
 // sqrt(a) for a positive normal double, without a library call: an FP32 reciprocal square
 // root of the mantissa (exponent split off on the integer pipe, a = a' 4^k with a' in [1, 4))
 // seeds Heron's iteration s <- s + (a - s^2) / (2 s), with 1 / (2 s) taken from the seed;

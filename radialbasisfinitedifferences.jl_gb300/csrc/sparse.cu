@@ -445,7 +445,7 @@ __device__ __forceinline__ typename Vec16<T>::V row_vec(int64_t a, int len, int 
 }
 
 // RK4 stage (same modes as rk4_stage_kernel) with 16-byte field vectors: F / Vec16::N lanes
-// per row, 32 / that rows per warp, rows in Z-order chunks of 64 per CTA.  Needs F a multiple
+// per row, 32 / that rows per warp, rows in Z-order chunks of (at least) 64 per CTA.  Needs F a multiple
 // of Vec16::N with F / Vec16::N dividing 32.
 template <typename T>
 __global__ void __launch_bounds__(256) rk4_stage_vec_kernel(int64_t rows, const int32_t *__restrict__ order,
@@ -459,10 +459,13 @@ __global__ void __launch_bounds__(256) rk4_stage_vec_kernel(int64_t rows, const 
     using V = typename VT::V;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int LPR = F / VT::N, RPW = 32 / LPR, sub = lane / LPR, sl = lane - sub * LPR;
-    const int64_t nchunk = (rows + 63) >> 6;
+    // chunks of CH consecutive rows of the order: 64, or one row group of the whole CTA when
+    // that is larger (8 warps x RPW rows)
+    const int CH = 8 * RPW > 64 ? 8 * RPW : 64;
+    const int64_t nchunk = (rows + CH - 1) / CH;
     for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
-        for (int k = 0; k < 64; k += 8 * RPW) {
-            const int64_t idx = ch * 64 + k + wib * RPW + sub;
+        for (int k = 0; k < CH; k += 8 * RPW) {
+            const int64_t idx = ch * CH + k + wib * RPW + sub;
             const bool valid = idx < rows;
             const int64_t r = valid ? (order ? (int64_t)order[idx] : idx) : 0;
             const int64_t a = valid ? row_ptr[r] : 0;
@@ -618,6 +621,160 @@ __global__ void lsq_update_p(int64_t cols, double *__restrict__ p, const double 
     const double beta = (!first && sc[0] > 0.0) ? sc[2] / sc[0] : 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cols; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = fma(beta, p[i], s[i]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Ghost-node closure (examples/adv_diff_test.jl:108-141, 160-176): u[G] = -inv(A[B,G]) A[B,~G] u.
+// gidx[node] = position of the node in G, -1 otherwise.
+
+// Left half of [W | I] (nb x 2nb, row-major): W[i][j] = A[B[i], G[j]], thread per boundary row.
+__global__ void ghost_extract_kernel(int64_t nb, const int32_t *__restrict__ bnodes, const int64_t *__restrict__ row_ptr,
+                                     const int32_t *__restrict__ col, const double *__restrict__ val,
+                                     const int32_t *__restrict__ gidx, double *__restrict__ W)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = bnodes[i];
+        for (int64_t t = row_ptr[r]; t < row_ptr[r + 1]; t++) {
+            const int j = gidx[col[t]];
+            if (j >= 0) W[i * 2 * nb + j] += val[t];
+        }
+    }
+}
+
+// Gauss-Jordan on [W | I] (nb x 2nb), step c: pivot row search by one block (largest |W[i][c]|
+// over rows i >= c, lowest row on ties), swap into row c.
+__global__ void gj_pivot_kernel(int64_t nb, double *__restrict__ M, int c, int *__restrict__ flag)
+{
+    __shared__ unsigned long long bk[256];
+    __shared__ int bi[256];
+    unsigned long long best = 0;
+    int brow = INT_MAX;
+    for (int64_t i = c + threadIdx.x; i < nb; i += blockDim.x) {
+        const unsigned long long k = (unsigned long long)__double_as_longlong(M[i * 2 * nb + c]) & 0x7fffffffffffffffull;
+        if (k > best || (k == best && (int)i < brow)) {
+            best = k;
+            brow = (int)i;
+        }
+    }
+    bk[threadIdx.x] = best;
+    bi[threadIdx.x] = brow;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            const unsigned long long k = bk[threadIdx.x + o];
+            const int r = bi[threadIdx.x + o];
+            if (k > bk[threadIdx.x] || (k == bk[threadIdx.x] && r < bi[threadIdx.x])) {
+                bk[threadIdx.x] = k;
+                bi[threadIdx.x] = r;
+            }
+        }
+        __syncthreads();
+    }
+    const int p = bi[0];
+    if (bk[0] == 0ull || bk[0] >= 0x7ff0000000000000ull) {
+        if (threadIdx.x == 0) *flag = 1;  // singular (zero, inf or NaN pivot)
+        return;
+    }
+    if (p != c)
+        for (int64_t j = threadIdx.x; j < 2 * nb; j += blockDim.x) {
+            const double t = M[(int64_t)c * 2 * nb + j];
+            M[(int64_t)c * 2 * nb + j] = M[(int64_t)p * 2 * nb + j];
+            M[(int64_t)p * 2 * nb + j] = t;
+        }
+}
+
+// Step c: multipliers fcol[i] = M[i][c] / M[c][c] of every other row.
+__global__ void gj_factors_kernel(int64_t nb, const double *__restrict__ M, int c, const int *__restrict__ flag,
+                                  double *__restrict__ fcol)
+{
+    if (*flag) return;
+    const int64_t w = 2 * nb;
+    const double rp = 1.0 / M[(int64_t)c * w + c];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
+        fcol[i] = i == c ? 0.0 : M[i * w + c] * rp;
+}
+
+// Step c: eliminate column c from every other row with the (unscaled) pivot row, thread per
+// element of the augmented matrix (column c itself is cleared by gj_finish_kernel).
+__global__ void gj_eliminate_kernel(int64_t nb, double *__restrict__ M, int c, const int *__restrict__ flag,
+                                    const double *__restrict__ fcol)
+{
+    if (*flag) return;
+    const int64_t w = 2 * nb;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nb * w; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / w, j = e - i * w;
+        if (i == c || j == c) continue;
+        M[i * w + j] = fma(-fcol[i], M[(int64_t)c * w + j], M[i * w + j]);
+    }
+}
+
+// Step c: clear column c of the other rows and divide the pivot row by its pivot (the pivot
+// element itself is left: column c is not read again).
+__global__ void gj_finish_kernel(int64_t nb, double *__restrict__ M, int c, const int *__restrict__ flag)
+{
+    if (*flag) return;
+    const int64_t w = 2 * nb;
+    const double rp = 1.0 / M[(int64_t)c * w + c];
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < w; j += (int64_t)gridDim.x * blockDim.x) {
+        if (j != c) M[(int64_t)c * w + j] *= rp;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
+        if (i != c) M[i * w + c] = 0.0;
+}
+
+// y[i][f] = sum over row B[i] of A, columns outside G, of val * u[col][f] (warp per row).
+template <typename T>
+__global__ void __launch_bounds__(256) ghost_rows_kernel(int64_t nb, const int32_t *__restrict__ bnodes,
+                                                         const int64_t *__restrict__ row_ptr,
+                                                         const int32_t *__restrict__ col, const double *__restrict__ val,
+                                                         const int32_t *__restrict__ gidx, const T *__restrict__ u,
+                                                         int F, double *__restrict__ y)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < nb; i += nw) {
+        const int64_t r = bnodes[i];
+        for (int f = lane; f < F; f += 32) {
+            double acc = 0.0;
+            for (int64_t t = row_ptr[r]; t < row_ptr[r + 1]; t++) {
+                const int c = col[t];
+                if (gidx[c] < 0) acc = fma(val[t], (double)u[(int64_t)c * F + f], acc);
+            }
+            y[i * F + f] = acc;
+        }
+    }
+}
+
+// u[G[j]][f] = -sum_i Winv[j][i] y[i][f] (Winv = the right half of the reduced [W | I]).
+template <typename T>
+__global__ void ghost_write_kernel(int64_t nb, const int32_t *__restrict__ gnodes, const double *__restrict__ M,
+                                   const double *__restrict__ y, int F, T *__restrict__ u)
+{
+    const int64_t w = 2 * nb;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nb * F; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / F;
+        const int f = (int)(e - j * F);
+        double acc = 0.0;
+        for (int64_t i = 0; i < nb; i++) acc = fma(M[j * w + nb + i], y[i * F + f], acc);
+        u[(int64_t)gnodes[j] * F + f] = (T)(-acc);
+    }
+}
+
+__global__ void ghost_index_kernel(int64_t nb, const int32_t *__restrict__ gnodes, int32_t *__restrict__ gidx)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nb; j += (int64_t)gridDim.x * blockDim.x)
+        gidx[gnodes[j]] = (int32_t)j;
+}
+
+__global__ void fill_i32_kernel(int64_t n, int32_t *a, int32_t v)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+__global__ void eye_right_kernel(int64_t nb, double *M)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
+        M[i * 2 * nb + nb + i] = 1.0;
 }
 
 // val_out = sum_q coef[q] * val_q (operators with one sparsity pattern), in FP64 and FP32.
@@ -889,6 +1046,42 @@ cudaError_t launch_lsq_update_p(int64_t cols, double *p, const double *s, const 
 }
 
 int lsq_partials() { return LSQ_BLOCKS; }
+
+// Dense inverse of the ghost block: [W | I] in M (nb x 2nb, row-major) reduced to [I | W^-1].
+cudaError_t ghost_build(int64_t N, int64_t nb, const int32_t *bnodes, const int32_t *gnodes, const int64_t *row_ptr,
+                        const int32_t *col, const double *val, int32_t *gidx, double *M, double *fcol, int *flag,
+                        cudaStream_t st)
+{
+    fill_i32_kernel<<<blocks_for(N, 256), 256, 0, st>>>(N, gidx, -1);
+    ghost_index_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(nb, gnodes, gidx);
+    cudaError_t e = cudaMemsetAsync(M, 0, sizeof(double) * nb * 2 * nb, st);
+    if (e != cudaSuccess) return e;
+    ghost_extract_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(nb, bnodes, row_ptr, col, val, gidx, M);
+    eye_right_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(nb, M);
+    for (int c = 0; c < (int)nb; c++) {
+        gj_pivot_kernel<<<1, 256, 0, st>>>(nb, M, c, flag);
+        gj_factors_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(nb, M, c, flag, fcol);
+        gj_eliminate_kernel<<<blocks_for(nb * 2 * nb, 256), 256, 0, st>>>(nb, M, c, flag, fcol);
+        gj_finish_kernel<<<blocks_for(2 * nb, 256), 256, 0, st>>>(nb, M, c, flag);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t ghost_apply(int64_t nb, const int32_t *bnodes, const int32_t *gnodes, const int64_t *row_ptr,
+                        const int32_t *col, const double *val, const int32_t *gidx, const double *M, void *u, int F,
+                        int dtype, double *y, cudaStream_t st)
+{
+    if (nb <= 0) return cudaSuccess;
+    const int blocks = blocks_for(nb * 32, 256);
+    if (dtype == 0) {
+        ghost_rows_kernel<double><<<blocks, 256, 0, st>>>(nb, bnodes, row_ptr, col, val, gidx, (const double *)u, F, y);
+        ghost_write_kernel<double><<<blocks_for(nb * F, 256), 256, 0, st>>>(nb, gnodes, M, y, F, (double *)u);
+    } else {
+        ghost_rows_kernel<float><<<blocks, 256, 0, st>>>(nb, bnodes, row_ptr, col, val, gidx, (const float *)u, F, y);
+        ghost_write_kernel<float><<<blocks_for(nb * F, 256), 256, 0, st>>>(nb, gnodes, M, y, F, (float *)u);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col, const void *val,
                         const void *x, void *y, int nfields, int dtype, cudaStream_t st)

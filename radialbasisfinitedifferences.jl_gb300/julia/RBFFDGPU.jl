@@ -311,6 +311,46 @@ function step!(rk::RK4, u, dt, nsteps)
     return u
 end
 
-export generate_operator, hyperviscosity_operator, calculateneighbors, OperatorSet, spmv!, RK4, step!
+"""
+    DeviceOperator(set, op)
+
+One operator of a device-resident set as a lazily materialised matrix: products with device
+vectors run on the GPU (`mul!` -> rbffd_spmv) and the host `SparseMatrixCSC` is built only
+when asked for (`SparseMatrixCSC(A)` -> rbffd_opset_export_csc into Julia-owned arrays, the
+same 1-based CSC the reference's `sparse(I, J, V)` returns), so a time loop never copies the
+operator to the host.
+"""
+struct DeviceOperator <: AbstractMatrix{Float64}
+    set::OperatorSet
+    op::Symbol
+end
+
+function shape(s::OperatorSet)
+    r, c, z, q = Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0), Ref{Cint}(0)
+    ccall((:rbffd_opset_shape, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Int64}, Ref{Cint}),
+          s.ptr, r, c, z, q)
+    return r[], c[], z[]
+end
+
+Base.size(A::DeviceOperator) = shape(A.set)[1:2]
+Base.getindex(A::DeviceOperator, i::Int, j::Int) = SparseMatrixCSC(A)[i, j]  # host access materialises
+
+LinearAlgebra.mul!(y, A::DeviceOperator, x) = spmv!(y, A.set, A.op, x)
+
+function SparseArrays.SparseMatrixCSC(A::DeviceOperator)
+    rows, cols, nnz = shape(A.set)
+    colptr, rowval, nzval = Vector{Int64}(undef, cols + 1), Vector{Int64}(undef, nnz), Vector{Float64}(undef, nnz)
+    q = findfirst(==(A.op), A.set.ops) - 1
+    GC.@preserve colptr rowval nzval begin
+        out = Ref(CSC(pointer(colptr), pointer(rowval), pointer(nzval)))
+        rc = ccall((:rbffd_opset_export_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{CSC}),
+                   A.set.h.ptr, A.set.ptr, q, out)
+    end
+    check(A.set.h, rc, Ref(Stats()))
+    return SparseMatrixCSC(rows, cols, colptr, rowval, nzval)
+end
+
+export generate_operator, hyperviscosity_operator, calculateneighbors, OperatorSet, spmv!, RK4, step!,
+       DeviceOperator
 
 end # module

@@ -221,6 +221,53 @@ def calculateneighbors(X, Y, n, X_idx_in=None, X_idx_bc=(), X_idx_bc_g=(), Y_idx
     return ix, iy, dx, dy
 
 
+class GhostClosure:
+    """Ghost-node closure of one boundary (rbffd_ghost_*): u[G] = -inv(A[B,G]) A[B,~G] u with A
+    one operator of a collocated set, B the boundary nodes and G their ghosts
+    (examples/adv_diff_test.jl:108-141, 160-176)."""
+
+    def __init__(self, opset, op, bnodes, gnodes, handle=None):
+        self.h = handle or opset.h
+        self._lib = nat.load()
+        self.opset = opset
+        b = np.ascontiguousarray(bnodes, dtype=np.int32)
+        g = np.ascontiguousarray(gnodes, dtype=np.int32)
+        if b.shape != g.shape:
+            raise ValueError("one ghost per boundary node")
+        out = ctypes.c_void_p()
+        nat.check(self.h.ptr, self._lib.rbffd_ghost_create(self.h.ptr, opset.ptr, opset.op_index(op), _ptr(b), _ptr(g),
+                                                           len(b), ctypes.byref(out)))
+        self.ptr = out
+
+    def apply(self, u):
+        """u: CUDA tensor [rows, nfields] (float64 or float32), ghost rows overwritten in place."""
+        import torch
+
+        dtype = 0 if u.dtype == torch.float64 else 1
+        torch.cuda.current_stream().synchronize()
+        nat.check(self.h.ptr, self._lib.rbffd_ghost_apply(self.h.ptr, self.ptr, ctypes.c_void_p(u.data_ptr()),
+                                                          u.shape[1] if u.dim() > 1 else 1, dtype))
+        self.h.synchronize()
+        return u
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self._lib.rbffd_ghost_destroy(self.h.ptr, self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class RK4Stepper:
     """Explicit RK4 for du/dt = L u with L = sum_i coef[i] A_i over the operators of one or
     more OperatorSets sharing a stencil pattern (rbffd_rk4_*): the time-stepping loop of
@@ -242,6 +289,12 @@ class RK4Stepper:
         nat.check(self.h.ptr, rc)
         self.ptr = out
         self.nfields = nfields
+
+    def set_closures(self, closures):
+        """Ghost closures applied to every stage input (rbffd_rk4_set_closure)."""
+        self._closures = list(closures)
+        arr = (ctypes.c_void_p * max(1, len(self._closures)))(*[c.ptr.value for c in self._closures])
+        nat.check(self.h.ptr, self._lib.rbffd_rk4_set_closure(self.h.ptr, self.ptr, arr, len(self._closures)))
 
     def run(self, u, dt, nsteps):
         """u: CUDA tensor [rows, nfields] (float64 or float32 to match dtype), advanced in place."""

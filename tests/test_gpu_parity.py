@@ -306,6 +306,86 @@ def test_spmv_sell_tiles(pkg, gpu):
             assert np.abs(yd.cpu().numpy() - yr).max() <= 1e-12 * np.abs(yr).max(), o
 
 
+def _ghost_problem(pkg):
+    d = pkg.nodesets.rectangle_with_ghosts(total=6000, seed=21, main_fraction=1.0)
+    X, cls = d["X"], d["node_class"]
+    s = pkg.OperatorSet(X, None, 3, 30, 3, ops=("Dx", "Dy"), node_class=cls)
+    # boundary b's nodes and its ghosts in matching order (ghost j sits outside boundary node j)
+    B = {b: np.nonzero(cls == b)[0] for b in (1, 2, 3, 4)}
+    G = {b: np.nonzero(cls == -b)[0] for b in (1, 2, 3, 4)}
+    return X, cls, s, B, G
+
+
+@pytest.mark.parametrize("dtype,tol", [("f64", 1e-10), ("f32", 1e-4)])
+def test_ghost_closure_matches_dense_inverse(pkg, gpu, dtype, tol):
+    """u[G] = -inv(A[B,G]) A[B,~G] u (examples/adv_diff_test.jl:108-141,160-176) against numpy,
+    for the right (Dx) and top (Dy) boundaries, and A[B,:] u = 0 afterwards."""
+    import torch
+
+    X, cls, s, B, G = _ghost_problem(pkg)
+    with s:
+        F = 3
+        rng = np.random.default_rng(2)
+        U = rng.standard_normal((len(X), F))
+        for b, op in ((2, "Dx"), (3, "Dy")):
+            A = s.csr(op)
+            Wg = A[B[b]][:, G[b]].toarray()
+            mask = np.ones(len(X), bool)
+            mask[G[b]] = False
+            Wint = A[B[b]][:, mask]
+            ref = U.copy()
+            ref[G[b]] = -np.linalg.solve(Wg, Wint @ U[mask])
+            td = torch.float64 if dtype == "f64" else torch.float32
+            ud = torch.tensor(U, dtype=td, device="cuda")
+            with pkg.GhostClosure(s, op, B[b], G[b]) as g:
+                g.apply(ud)
+            got = ud.double().cpu().numpy()
+            assert np.abs(got - ref).max() <= tol * np.abs(ref).max(), (b, op)
+            if dtype == "f64":
+                assert np.abs(A[B[b]] @ got).max() <= 1e-8 * np.abs(A[B[b]]).sum(1).max() * np.abs(got).max()
+
+
+def test_rk4_with_ghost_closure(pkg, gpu):
+    """RK4 with the closure applied to every stage input against the same scheme in numpy."""
+    import scipy.sparse as sp
+    import torch
+
+    X, cls, s, B, G = _ghost_problem(pkg)
+    with s:
+        coef = [-1.0, -0.5]
+        L = coef[0] * s.csr("Dx") + coef[1] * s.csr("Dy")
+        Ax = s.csr("Dx")
+        mask = np.ones(len(X), bool)
+        mask[G[2]] = False
+        Wg = Ax[B[2]][:, G[2]].toarray()
+        Wint = Ax[B[2]][:, mask]
+
+        def close(v):
+            v = v.copy()
+            v[G[2]] = -np.linalg.solve(Wg, Wint @ v[mask])
+            return v
+
+        F, dt, nsteps = 2, 1e-4, 5
+        U0 = np.random.default_rng(3).standard_normal((len(X), F))
+        u = U0.copy()
+        for _ in range(nsteps):
+            u = close(u)
+            k1 = L @ u
+            w = close(u + 0.5 * dt * k1)
+            k2 = L @ w
+            w = close(u + 0.5 * dt * k2)
+            k3 = L @ w
+            w = close(u + dt * k3)
+            k4 = L @ w
+            u = u + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        with pkg.GhostClosure(s, "Dx", B[2], G[2]) as g, pkg.RK4Stepper([s], coef, F, "f64") as st:
+            st.set_closures([g])
+            ud = torch.tensor(U0, device="cuda")
+            st.run(ud, dt, nsteps)
+            got = ud.cpu().numpy()
+        assert np.abs(got - u).max() <= 1e-9 * np.abs(u).max()
+
+
 def test_row_range_shards(pkg, orc, gpu):
     X, _ = grid(pkg, 40, seed=4)
     p, n, deg = 3, 20, 3
@@ -339,12 +419,13 @@ def test_errors(pkg, gpu):
     assert np.allclose(E.toarray(), np.eye(len(X)), atol=1e-10)
 
 
-@pytest.mark.parametrize("F", [5, 64])
+@pytest.mark.parametrize("F", [2, 5, 64])
 @pytest.mark.parametrize("dtype,tol", [("f64", 1e-10), ("f32", 2e-5)])
 def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol, F):
     """RK4 of du/dt = L u, L = -Dx - 0.5 Dy + 0.01 Lap, boundary band held fixed, against a
     numpy RK4 with the oracle's operators (7 steps: three graph-replayed pairs + one).  F = 5
-    takes the lane-per-field kernels, F = 64 the 16-byte field-vector kernels."""
+    takes the lane-per-field kernels, F = 2 and 64 the 16-byte field-vector kernels (32 and 1-2
+    rows per warp)."""
     import scipy.sparse as sp
     import torch
 
