@@ -429,6 +429,22 @@ __device__ __forceinline__ typename Vec16<T>::V row_vec(int64_t a, int len, int 
         }
         const int cnt = lenmax - t0 < LPR ? lenmax - t0 : LPR;
         int t = 0;
+        for (; t + 4 <= cnt; t += 4) {  // four independent gathers in flight
+            int c[4];
+            T wv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = __shfl_sync(0xffffffffu, cl, t + u, LPR);
+                wv[u] = __shfl_sync(0xffffffffu, wl, t + u, LPR);
+            }
+            typename VT::V xg[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) xg[u] = __ldg(xv + (int64_t)c[u] * FV);
+            s0 = VT::fma1(wv[0], xg[0], s0);
+            s1 = VT::fma1(wv[1], xg[1], s1);
+            s0 = VT::fma1(wv[2], xg[2], s0);
+            s1 = VT::fma1(wv[3], xg[3], s1);
+        }
         for (; t + 2 <= cnt; t += 2) {
             const int c0 = __shfl_sync(0xffffffffu, cl, t, LPR), c1 = __shfl_sync(0xffffffffu, cl, t + 1, LPR);
             const T w0 = __shfl_sync(0xffffffffu, wl, t, LPR), w1 = __shfl_sync(0xffffffffu, wl, t + 1, LPR);
