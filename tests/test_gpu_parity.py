@@ -75,7 +75,8 @@ def test_weights_all_ops(pkg, orc, gpu, precision, tol):
             assert rel_row_err(val, ref["W"][ops.index(o)]) < tol, o
 
 
-@pytest.mark.parametrize("cfg", [(3, 30, 3), (3, 20, 2), (5, 42, 5), (3, 45, 4), (3, 60, 5)])
+@pytest.mark.parametrize("cfg", [(3, 30, 3), (3, 20, 2), (5, 42, 5), (3, 45, 4), (3, 60, 5), (1, 5, 0), (3, 8, 1),
+                                 (7, 32, 3), (3, 33, 3), (3, 64, 5)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_weights_sizes(pkg, orc, gpu, cfg, precision):
     p, n, deg = cfg
@@ -87,6 +88,21 @@ def test_weights_sizes(pkg, orc, gpu, cfg, precision):
             _, col, val = s.csr_arrays(o)
             assert (col.reshape(-1, n) == ref["cols"]).all()
             assert rel_row_err(val, ref["W"][ops.index(o)]) < tol_for(p, deg, precision), o
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_weights_noncollocated(pkg, orc, gpu, precision):
+    """Y != X: evaluation points reuse the factorisation of their nearest node (several rows per
+    local system), src/generate_operator.jl:47,89-167."""
+    X, _ = grid(pkg, 40, seed=6)
+    Y = np.random.default_rng(7).uniform(0.02, 0.98, (3000, 2))
+    ops = ("E", "Dx", "Dy", "Lap")
+    ref = orc.generate(X, Y, 3, 20, 3, ops)
+    with pkg.OperatorSet(X, Y, 3, 20, 3, ops=ops, precision=precision) as s:
+        for o in s.ops:
+            _, col, val = s.csr_arrays(o)
+            assert (col.reshape(-1, 20) == ref["cols"]).all()
+            assert rel_row_err(val, ref["W"][ops.index(o)]) < tol_for(3, 3, precision), o
 
 
 def test_hyperviscosity_weights(pkg, orc, gpu):
