@@ -19,6 +19,8 @@ struct rbffd_handle {
     std::string err;
     int num_sms = 0;
     cudaEvent_t ev[8] = {};
+    cudaStream_t side = nullptr;  // overlaps the CSC export pattern with the weight solves
+    cudaEvent_t side_ev[2] = {};
 };
 
 struct rbffd_opset {
@@ -484,6 +486,13 @@ RBFFD_EXPORT int rbffd_create(const rbffd_options *opt, rbffd_handle **out)
         return RBFFD_ECUDA;
     }
     for (auto &ev : h->ev) cudaEventCreate(&ev);
+    if ((e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking)) != cudaSuccess) {
+        g_create_error = std::string("cuda: ") + cudaGetErrorString(e);
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return RBFFD_ECUDA;
+    }
+    for (auto &ev : h->side_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     *out = h;
     return RBFFD_OK;
 }
@@ -493,8 +502,11 @@ RBFFD_EXPORT void rbffd_destroy(rbffd_handle *h)
     if (!h) return;
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->side);
     for (auto &ev : h->ev) cudaEventDestroy(ev);
+    for (auto &ev : h->side_ev) cudaEventDestroy(ev);
     cudaStreamDestroy(h->stream);
+    cudaStreamDestroy(h->side);
     delete h;
 }
 
@@ -516,8 +528,18 @@ RBFFD_EXPORT int rbffd_synchronize(rbffd_handle *h)
 // ---------------------------------------------------------------------------
 // Operator sets.
 // ---------------------------------------------------------------------------
+// Used by opset_build for a collocated uniform set, whose CSR pattern is known before the
+// weights (col = nbr, row r at r * n): build() runs on the main stream before the weight
+// solves are launched, download() after they are enqueued (copies on the side stream overlap
+// the solves).  The drop-in calls use it for the CSC pattern of their outputs.
+struct PatternHook {
+    virtual int build(rbffd_handle *h, int64_t N, int n, const int64_t *row_ptr, const int32_t *nbr) = 0;
+    virtual int download(rbffd_handle *h) = 0;
+    virtual ~PatternHook() {}
+};
+
 static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, rbffd_opset **out,
-                       rbffd_stats *stats)
+                       rbffd_stats *stats, PatternHook *hook = nullptr)
 {
     if (!h) return RBFFD_EINVAL;
     if (!pb || !out) return fail(h, RBFFD_EINVAL, "null argument");
@@ -690,6 +712,11 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         CK(cudaMemcpyAsync(&nnz, row_ptr + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
     }
+    const bool hook_on = hook && collocated && uniform && rb == 0 && rows == N;
+    if (hook_on) {
+        int rc2 = hook->build(h, N, pb->n, row_ptr, nbr);
+        if (rc2) return bail(rc2);
+    }
     int32_t *col;
     double *val;
     CK(keep.get(&col, nnz));
@@ -773,6 +800,10 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     } else {
         int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
         CK(launch_solve_fp64(a, table, wpb, h->num_sms, st));
+    }
+    if (hook_on) {
+        int rc2 = hook->download(h);
+        if (rc2) return bail(rc2);
     }
     CK(cudaEventRecord(h->ev[4], st));
     Flags hf;
@@ -1457,6 +1488,107 @@ static int export_all(rbffd_handle *h, rbffd_opset *s, rbffd_csc *out)
     return RBFFD_OK;
 }
 
+// The CSC pattern of a collocated uniform set depends on the stencils only, so the drop-in
+// calls build it before the weight solves and download colptr/rowval into every output on the
+// side stream while the solves run; the values follow once the solves finish.
+struct EarlyCsc : PatternHook {
+    rbffd_csc *out = nullptr;
+    int nops = 0;
+    int64_t N = 0, nnz = 0;
+    int64_t *colstart = nullptr, *rowval = nullptr, *perm = nullptr;
+    bool active = false;
+
+    int build(rbffd_handle *h, int64_t N_, int n, const int64_t *row_ptr, const int32_t *nbr) override
+    {
+        cudaStream_t st = h->stream;
+        N = N_;
+        nnz = N_ * n;
+        int64_t *count, *fill;
+        void *scratch;
+        const size_t tb = scan_tmp_bytes(N);
+        CK(cudaMallocAsync((void **)&count, sizeof(int64_t) * (N + 1), st));
+        CK(cudaMallocAsync((void **)&fill, sizeof(int64_t) * N, st));
+        CK(cudaMallocAsync(&scratch, tb, st));
+        CK(cudaMallocAsync((void **)&colstart, sizeof(int64_t) * (N + 1), st));
+        CK(cudaMallocAsync((void **)&rowval, sizeof(int64_t) * nnz, st));
+        CK(cudaMallocAsync((void **)&perm, sizeof(int64_t) * nnz, st));
+        active = true;
+        CK(cudaMemsetAsync(count, 0, sizeof(int64_t) * (N + 1), st));
+        CK(cudaMemsetAsync(fill, 0, sizeof(int64_t) * N, st));
+        CK(launch_csc_count(nnz, nbr, count, st));
+        CK(scan_exclusive_i64(count, colstart, N, scratch, tb, st));
+        CK(launch_csc_scatter(N, row_ptr, nbr, 0, colstart, fill, rowval, perm, st));
+        CK(launch_csc_sort_segments(N, colstart, rowval, perm, st));
+        CK(launch_add_i64(N + 1, colstart, 1, st));  // Julia is 1-based
+        CK(launch_add_i64(nnz, rowval, 1, st));
+        CK(cudaFreeAsync(count, st));
+        CK(cudaFreeAsync(fill, st));
+        CK(cudaFreeAsync(scratch, st));
+        CK(cudaEventRecord(h->side_ev[0], st));
+        return RBFFD_OK;
+    }
+
+    int download(rbffd_handle *h) override
+    {
+        cudaStream_t ss = h->side;
+        CK(cudaStreamWaitEvent(ss, h->side_ev[0], 0));
+        for (int q = 0; q < nops; q++) {
+            if (out[q].colptr)
+                CK(cudaMemcpyAsync(out[q].colptr, colstart, sizeof(int64_t) * (N + 1), cudaMemcpyDeviceToHost, ss));
+            if (out[q].rowval)
+                CK(cudaMemcpyAsync(out[q].rowval, rowval, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, ss));
+        }
+        CK(cudaEventRecord(h->side_ev[1], ss));
+        return RBFFD_OK;
+    }
+
+    void release(rbffd_handle *h)
+    {
+        cudaStreamSynchronize(h->side);
+        if (colstart) cudaFreeAsync(colstart, h->side);
+        if (rowval) cudaFreeAsync(rowval, h->side);
+        if (perm) cudaFreeAsync(perm, h->side);
+        cudaStreamSynchronize(h->side);
+        colstart = rowval = perm = nullptr;
+    }
+};
+
+// Build the operator set of a drop-in call and write its CSC matrices into `out`.
+static int build_and_export(rbffd_handle *h, const rbffd_problem *pb, int unscaled, rbffd_csc *out,
+                            rbffd_stats *stats)
+{
+    rbffd_opset *s = nullptr;
+    EarlyCsc ec;
+    ec.out = out;
+    ec.nops = __builtin_popcount(pb->op_mask);
+    int rc = opset_build(h, pb, unscaled, &s, stats, &ec);
+    if (rc) {
+        ec.release(h);
+        return rc;
+    }
+    if (ec.active) {
+        cudaStream_t st = h->stream;
+        double *buf = nullptr;
+        cudaError_t e = cudaStreamWaitEvent(st, h->side_ev[1], 0);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&buf, sizeof(double) * s->nnz, st);
+        for (int q = 0; q < s->nops && e == cudaSuccess; q++) {
+            if (!out[q].nzval) continue;
+            e = launch_gather_f64(s->nnz, ec.perm, s->val + (size_t)q * s->nnz, buf, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(out[q].nzval, buf, sizeof(double) * s->nnz, cudaMemcpyDeviceToHost, st);
+        }
+        if (buf) cudaFreeAsync(buf, st);
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = e2;
+        rc = e == cudaSuccess ? RBFFD_OK : fail(h, RBFFD_ECUDA, std::string("csc export: ") + cudaGetErrorString(e));
+    } else {
+        rc = export_all(h, s, out);
+    }
+    ec.release(h);
+    rbffd_opset_destroy(h, s);
+    return rc;
+}
+
 RBFFD_EXPORT int rbffd_generate_operator(rbffd_handle *h, const double *X, int64_t N, const double *Y,
                                          int64_t M, int p, int n, int polydeg, const int32_t *node_class,
                                          uint32_t op_mask, int precision, rbffd_csc *out,
@@ -1476,12 +1608,7 @@ RBFFD_EXPORT int rbffd_generate_operator(rbffd_handle *h, const double *X, int64
     pb.op_mask = op_mask;
     pb.precision = precision;
     pb.memspace = RBFFD_MEM_HOST;
-    rbffd_opset *s = nullptr;
-    int rc = opset_build(h, &pb, 0, &s, stats);
-    if (rc) return rc;
-    rc = export_all(h, s, out);
-    rbffd_opset_destroy(h, s);
-    return rc;
+    return build_and_export(h, &pb, 0, out, stats);
 }
 
 RBFFD_EXPORT int rbffd_hyperviscosity_operator(rbffd_handle *h, int k_deriv, const double *X, int64_t N,
@@ -1504,12 +1631,7 @@ RBFFD_EXPORT int rbffd_hyperviscosity_operator(rbffd_handle *h, int k_deriv, con
     pb.k_deriv = k_deriv;
     pb.precision = precision;
     pb.memspace = RBFFD_MEM_HOST;
-    rbffd_opset *s = nullptr;
-    int rc = opset_build(h, &pb, 0, &s, stats);
-    if (rc) return rc;
-    rc = export_all(h, s, out);
-    rbffd_opset_destroy(h, s);
-    return rc;
+    return build_and_export(h, &pb, 0, out, stats);
 }
 
 RBFFD_EXPORT int rbffd_generate_operator_unscaled(rbffd_handle *h, const double *X, int64_t N, int p, int n,
