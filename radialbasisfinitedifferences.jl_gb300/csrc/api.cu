@@ -1010,7 +1010,7 @@ RBFFD_EXPORT int rbffd_spmv(rbffd_handle *h, rbffd_opset *s, int op, const doubl
                             h->stream));
         return RBFFD_OK;
     }
-    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, 0, h->num_sms, h->stream));
+    CK(launch_spmv_f64(s->rows, s->row_ptr, s->col, s->val + (size_t)op * s->nnz, x, y, h->num_sms, h->stream));
     return RBFFD_OK;
 }
 

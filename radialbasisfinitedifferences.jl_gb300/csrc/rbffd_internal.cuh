@@ -191,9 +191,9 @@ size_t solve_fp64_smem_per_warp(int max_s, int max_n, int nops);
 size_t solve_mixed_smem_per_warp(int max_s, int max_n, int nops);
 
 // Sparse kernels.
+// FP64 SpMV of a general CSR operator (thread per row); uniform stencils use the SELL-32 kernel.
 cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t *col,
-                            const double *val, const double *x, double *y, int group,
-                            int num_sms, cudaStream_t st);
+                            const double *val, const double *x, double *y, int num_sms, cudaStream_t st);
 cudaError_t launch_spmm(int64_t rows, const int64_t *row_ptr, const int32_t *col,
                         const void *val, const void *x, void *y, int nfields, int dtype,
                         cudaStream_t st);

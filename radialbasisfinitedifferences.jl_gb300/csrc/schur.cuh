@@ -38,15 +38,6 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 #ifndef RBFFD_SCHUR_MIN_BLOCKS
 #define RBFFD_SCHUR_MIN_BLOCKS 4
 #endif
-// 1: for stencils of <= 32 nodes the FP64 Phi passes run inside the first Gauss-Jordan steps
-// (reg_gj's hook).  Off by default: +1 % on uniform k = 30 batches, -8 % on mixed-size ones.
-#ifndef RBFFD_SCHUR_INTERLEAVE
-#define RBFFD_SCHUR_INTERLEAVE 0
-#endif
-// 1: residuals after the first are r - A d in double-float FP32 arithmetic (residual_df).
-#ifndef RBFFD_SCHUR_DF_RESIDUAL
-#define RBFFD_SCHUR_DF_RESIDUAL 1
-#endif
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
 template <int B, int E, typename F>
@@ -176,22 +167,14 @@ __device__ __forceinline__ void fill_phi_rows(RegRows<SP> &R, const float2 *x32,
 // row stays multiplied by its pivot (elimination is linear, so later updates apply unchanged)
 // and is divided by it once at the end, so each step is a uniform FMA sweep.  Fails on a
 // zero, subnormal, infinite or NaN pivot.
-struct NoHook {
-    __device__ void operator()(int) const {}
-};
-
-// `hook(c)` runs at the start of steps c < 8: independent work (the FP64 assembly) placed
-// there overlaps the latency of the elimination's FP32 chain.
-template <int S, typename Hook = NoHook>
-__device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *dinv, float *prow, int lane,
-                                       Hook &&hook = Hook())
+template <int S>
+__device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *dinv, float *prow, int lane)
 {
     constexpr int NS = RegRows<S>::NS;
     bool ok = true;
     static_for<0, S>([&](auto CC) {
         constexpr int c = decltype(CC)::value;
         if (c >= s || !ok) return;
-        if constexpr (c < 8) hook(c);  // the first 8 steps only: bounded code size
         unsigned key = 0u;
         int brow = INT_MAX;
 #pragma unroll
@@ -702,12 +685,12 @@ __device__ __forceinline__ void phi_pair_pass(const double *xs, int n, int p, do
     if (two) phiP[tt + i2] = v2;
 }
 
-// Passes [pass0, end) of the packed FP64 Phi, its zero diagonal and the FP64 P rows.
+// The packed FP64 Phi (two pairs per lane per pass), its zero diagonal and the FP64 P rows.
 __device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
-                                                    double *P, int pass0, int lane)
+                                                    double *P, int lane)
 {
     const int npass = (n * (n - 1) / 2 + 63) / 64;
-    for (int q = pass0; q < npass; q++) phi_pair_pass(xs, n, p, phiP, 64 * q, lane);
+    for (int q = 0; q < npass; q++) phi_pair_pass(xs, n, p, phiP, 64 * q, lane);
     for (int i = lane; i < n; i += 32) {
         phiP[tri_off(i) + i] = 0.0;
         monomial_row<double>(xs[2 * i], xs[2 * i + 1], deg, P + i * m, 1);
@@ -851,17 +834,10 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
         __syncwarp();
         RegRows<SP> RP;
         fill_phi_rows<SP>(RP, x32, n, p, lane);
-        // the FP64 Phi passes ride along the first Gauss-Jordan steps
-        const int npass = (n * (n - 1) / 2 + 63) / 64;
-        bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane, [&](int c) {
-            if (RBFFD_SCHUR_INTERLEAVE && SP <= 32 && c < npass) phi_pair_pass(xs, n, p, phiP, 64 * c, lane);
-        });
+        bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
         if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
         bool fallback = !ok;
-        if (ok) {
-            const int done = (RBFFD_SCHUR_INTERLEAVE && SP <= 32) ? (npass < 8 ? npass : 8) : 0;
-            assemble_phi_packed(xs, n, m, deg, p, phiP, P, done, lane);
-        }
+        if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, lane);
         int64_t r0, r1;
         system_rows(a, sys, j, r0, r1);
         int iters_max = 0;
@@ -877,8 +853,8 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                 if (it == 0) {
                     for (int e = lane; e < s * r; e += 32) R32[e] = f64_to_f32(B[e]);
                     __syncwarp();
-                } else if (it == 1 || !RBFFD_SCHUR_DF_RESIDUAL) {
-                    residual_schur(phiP, P, n, m, r, B, X, R32, RBFFD_SCHUR_DF_RESIDUAL != 0, lane);
+                } else if (it == 1) {
+                    residual_schur(phiP, P, n, m, r, B, X, R32, true, lane);
                 } else {
                     residual_df<SP, SM, RMAX>(phiP, P, n, m, r, B, R32, lane);
                 }

@@ -35,50 +35,6 @@ __global__ void __launch_bounds__(256) spmv_f64_rows(int64_t rows, const int64_t
     }
 }
 
-// Uniform stencil size K (even): row r occupies [r*K, r*K + K); 16-byte weight loads and
-// 8-byte index loads, fully unrolled.
-template <int K>
-__global__ void __launch_bounds__(256) spmv_f64_uniform(int64_t rows, const int32_t *__restrict__ col,
-                                                        const double *__restrict__ val,
-                                                        const double *__restrict__ x, double *__restrict__ y)
-{
-    static_assert(K % 2 == 0, "even K");
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        const double2 *v2 = reinterpret_cast<const double2 *>(val + r * K);
-        const int2 *c2 = reinterpret_cast<const int2 *>(col + r * K);
-        double2 w[K / 2];
-        int2 c[K / 2];
-#pragma unroll
-        for (int i = 0; i < K / 2; i++) {
-            w[i] = __ldcs(v2 + i);
-            c[i] = __ldcs(c2 + i);
-        }
-        double acc = 0.0;
-#pragma unroll
-        for (int i = 0; i < K / 2; i++) {
-            acc = fma(w[i].x, __ldg(x + c[i].x), acc);
-            acc = fma(w[i].y, __ldg(x + c[i].y), acc);
-        }
-        __stcs(y + r, acc);
-    }
-}
-
-// 16-byte asynchronous global -> shared copy that skips L1 and marks the line evict-first in
-// L2 (the streamed weights and column ids must not push the gathered x out of L2).
-__device__ __forceinline__ void cp_async16_stream(void *smem, const void *gmem, unsigned long long pol)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(pol)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // SELL-32 layout of a uniform-stencil operator (sliced ELLPACK with slice height 32, one warp):
 // slice (tile) i holds rows 32i..32i+31 column-major, entry t of row 32i + l at
 // (i*K + t)*32 + l, so the t-th weights and column ids of a warp's 32 rows are one contiguous
@@ -105,41 +61,20 @@ __global__ void __launch_bounds__(256) csr_to_sell_kernel(int64_t rows, int K, c
 // column-id load is a fully coalesced line, so no shared-memory staging is needed and the
 // kernel runs at full occupancy (the latency of the x gathers is hidden by warps, not
 // stages); each row accumulates in four independent FP64 chains.
-// Streamed read-only loads that the compiler may schedule freely (no volatile asm, so all of a
-// row's weight and column-id loads can be in flight together) with an L2 evict-first hint.
-#ifndef RBFFD_SELL_LOAD
-#define RBFFD_SELL_LOAD 2
-#endif
-#ifndef RBFFD_SELL_BATCH
-#define RBFFD_SELL_BATCH 10
-#endif
+// Streamed read-only loads with an L2 evict-first hint, written as non-volatile asm so that
+// the compiler may schedule them freely (all of a batch's weight and column-id loads in flight
+// together).
 __device__ __forceinline__ double ld_stream(const double *p, unsigned long long pol)
 {
-#if RBFFD_SELL_LOAD == 0
-    (void)pol;
-    return __ldcs(p);
-#elif RBFFD_SELL_LOAD == 1
-    (void)pol;
-    return __ldg(p);
-#else
     double v;
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
     return v;
-#endif
 }
 __device__ __forceinline__ int ld_stream(const int32_t *p, unsigned long long pol)
 {
-#if RBFFD_SELL_LOAD == 0
-    (void)pol;
-    return __ldcs(p);
-#elif RBFFD_SELL_LOAD == 1
-    (void)pol;
-    return __ldg(p);
-#else
     int v;
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
     return v;
-#endif
 }
 
 template <int K>
@@ -158,8 +93,9 @@ __global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const
         const double *v = sval + tile * 32 * k + lane;
         double a[4] = {0.0, 0.0, 0.0, 0.0};
         if constexpr (K > 0) {
-#if RBFFD_SELL_BATCH > 0
-            constexpr int BT = RBFFD_SELL_BATCH;
+            // batches of ten entries: the ten column/weight loads, then the ten x gathers, then
+            // the FMAs (65 % -> 75 % of HBM against one entry at a time)
+            constexpr int BT = 10;
 #pragma unroll
             for (int t0 = 0; t0 < K; t0 += BT) {
                 int cc[BT];
@@ -177,11 +113,6 @@ __global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const
                 for (int u = 0; u < BT; u++)
                     if (t0 + u < K) a[(t0 + u) & 3] = fma(vv[u], xx[u], a[(t0 + u) & 3]);
             }
-#else
-#pragma unroll
-            for (int t = 0; t < K; t++)
-                a[t & 3] = fma(ld_stream(v + 32 * t, pol), __ldg(x + ld_stream(c + 32 * t, pol)), a[t & 3]);
-#endif
         } else {
             int t = 0;
             for (; t + 4 <= k; t += 4) {
@@ -196,80 +127,6 @@ __global__ void __launch_bounds__(256) spmv_f64_sell(int64_t rows, int kr, const
     }
 }
 
-// Pipeline depth of the FP64 SpMV (tiles in flight per warp, including the one computed).
-#ifndef RBFFD_SPMV_STAGES
-#define RBFFD_SPMV_STAGES 3
-#endif
-
-// Uniform stencil size K (even), S-stage pipeline: each warp owns tiles of 32 consecutive
-// rows (weights 32*K doubles and column ids 32*K ints, contiguous and 16-byte aligned in HBM)
-// and keeps the next S-1 tiles in flight into its shared-memory stages with cp.async while
-// it computes the current one, so HBM streaming overlaps the FP64 FMAs (31.5M FMAs take
-// ~50 us at GB300's FP64 rate, about as long as streaming their 378 MB).  Each lane
-// accumulates its own row from shared memory in four independent chains; x is gathered
-// through L1/L2.
-template <int K, int S>
-__global__ void __launch_bounds__(256) spmv_f64_pipe(int64_t rows, const int32_t *__restrict__ col,
-                                                     const double *__restrict__ val,
-                                                     const double *__restrict__ x, double *__restrict__ y)
-{
-    static_assert(K % 2 == 0, "even K");
-    constexpr int VB = 32 * K * 8, CB = 32 * K * 4, STB = VB + CB;
-    extern __shared__ __align__(16) unsigned char sm_dyn[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned char *mine = sm_dyn + (size_t)w * S * STB;
-    unsigned long long pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
-    const int64_t ntile = (rows + 31) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t first = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-
-    auto issue = [&](int64_t tile, int stage) {
-        const int64_t r0 = tile * 32;
-        const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
-        double *sv = reinterpret_cast<double *>(mine + stage * STB);
-        int *sc = reinterpret_cast<int *>(mine + stage * STB + VB);
-        const double2 *gv = reinterpret_cast<const double2 *>(val + r0 * K);
-        const int nv2 = nr * K / 2;
-        for (int c = lane; c < nv2; c += 32) cp_async16_stream(reinterpret_cast<double2 *>(sv) + c, gv + c, pol);
-        const int nc = nr * K, nc4 = nc >> 2;
-        const int4 *gc = reinterpret_cast<const int4 *>(col + r0 * K);
-        for (int c = lane; c < nc4; c += 32) cp_async16_stream(reinterpret_cast<int4 *>(sc) + c, gc + c, pol);
-        for (int c = 4 * nc4 + lane; c < nc; c += 32) sc[c] = __ldcs(col + r0 * K + c);
-    };
-
-#pragma unroll
-    for (int k = 0; k < S - 1; k++) {
-        const int64_t t = first + k * nw;
-        if (t < ntile) issue(t, k);
-        cp_async_commit();
-    }
-    int stage = 0;
-    for (int64_t tile = first; tile < ntile; tile += nw) {
-        const int64_t nxt = tile + (S - 1) * nw;
-        if (nxt < ntile) issue(nxt, stage == 0 ? S - 1 : stage - 1);
-        cp_async_commit();
-        cp_async_wait<S - 1>();
-        __syncwarp();
-        const int64_t r0 = tile * 32;
-        const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
-        if (lane < nr) {
-            const double2 *mv = reinterpret_cast<const double2 *>(mine + stage * STB) + lane * (K / 2);
-            const int2 *mc = reinterpret_cast<const int2 *>(mine + stage * STB + VB) + lane * (K / 2);
-            double a[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-            for (int i = 0; i < K / 2; i++) {
-                const double2 wv = mv[i];
-                const int2 cv = mc[i];
-                a[(2 * i) & 3] = fma(wv.x, __ldg(x + cv.x), a[(2 * i) & 3]);
-                a[(2 * i + 1) & 3] = fma(wv.y, __ldg(x + cv.y), a[(2 * i + 1) & 3]);
-            }
-            __stcs(y + r0 + lane, (a[0] + a[1]) + (a[2] + a[3]));
-        }
-        __syncwarp();
-        stage = stage == S - 1 ? 0 : stage + 1;
-    }
-    cp_async_wait<0>();
-}
 
 // v[f] = sum_t val[t] x[col[t]][f] for one row, lanes over fields f = f0 + lane and f0 + lane + 32:
 // the row's column ids and weights are loaded once, coalesced (lane t holds entry t), and
@@ -940,57 +797,16 @@ bool vec_fields_ok(int F, int dtype, const void *a, const void *b, const void *c
     return ((((uintptr_t)a) | ((uintptr_t)b) | ((uintptr_t)c) | ((uintptr_t)d)) & 15u) == 0;
 }
 
-// One CTA of up to 8 warps per SM, each warp with RBFFD_SPMV_STAGES K-row-tile stages.
-template <int K>
-cudaError_t launch_spmv_pipe(int64_t rows, const int32_t *col, const double *val, const double *x, double *y,
-                             int num_sms, cudaStream_t st)
-{
-    constexpr int S = RBFFD_SPMV_STAGES;
-    const size_t per_warp = S * (size_t)32 * K * 12;
-    int dev = 0, smem_max = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    int wpb = (int)(smem_max / per_warp);
-    if (wpb > 8) wpb = 8;
-    if (wpb < 1) return cudaErrorNotSupported;
-    const size_t smem = per_warp * wpb;
-    auto kern = spmv_f64_pipe<K, S>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, wpb * 32, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-    const int64_t tiles = (rows + 31) / 32;
-    int64_t blocks = (int64_t)num_sms * occ;
-    const int64_t need = (tiles + wpb - 1) / wpb;
-    if (blocks > need) blocks = need;
-    kern<<<(int)blocks, wpb * 32, smem, st>>>(rows, col, val, x, y);
-    return cudaGetLastError();
-}
 
 }  // namespace
 
 cudaError_t launch_spmv_f64(int64_t rows, const int64_t *row_ptr, const int32_t *col,
-                            const double *val, const double *x, double *y, int group, int num_sms,
-                            cudaStream_t st)
+                            const double *val, const double *x, double *y, int num_sms, cudaStream_t st)
 {
     if (rows <= 0) return cudaSuccess;
-    int threads = 256;
-    int blocks = blocks_for(rows, threads, (int64_t)num_sms * 64);
-    // `group` carries the uniform stencil size (0 = general CSR)
-    switch (group) {
-    case 20: spmv_f64_uniform<20><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
-    case 30:
-        // cp.async needs 16-byte aligned tiles (true for the library's own arrays)
-        if ((((uintptr_t)val) | ((uintptr_t)col)) & 15u)
-            spmv_f64_uniform<30><<<blocks, threads, 0, st>>>(rows, col, val, x, y);
-        else
-            return launch_spmv_pipe<30>(rows, col, val, x, y, num_sms, st);
-        break;
-    case 42: spmv_f64_uniform<42><<<blocks, threads, 0, st>>>(rows, col, val, x, y); break;
-    default: spmv_f64_rows<<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y); break;
-    }
+    const int threads = 256;
+    const int blocks = blocks_for(rows, threads, (int64_t)num_sms * 64);
+    spmv_f64_rows<<<blocks, threads, 0, st>>>(rows, row_ptr, col, val, x, y);
     return cudaGetLastError();
 }
 
