@@ -659,38 +659,56 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
     __syncwarp();
 }
 
-// One pass of the packed FP64 Phi: strictly lower pairs t0 + lane and t0 + 32 + lane
-// (row-major: t = i (i - 1) / 2 + j, stored at tri_off(i) + j = t + i).
+// (i, j) of the t-th strictly lower pair (row-major: t = i (i - 1) / 2 + j) for stencils of
+// up to 64 nodes, as (i << 8) | j: one cached load instead of a square root and fix-ups.
+struct PairTable {
+    uint16_t ij[64 * 63 / 2];
+};
+constexpr PairTable make_pair_table()
+{
+    PairTable T{};
+    int t = 0;
+    for (int i = 1; i < 64; i++)
+        for (int j = 0; j < i; j++) T.ij[t++] = (uint16_t)((i << 8) | j);
+    return T;
+}
+__device__ const PairTable g_pair_table = make_pair_table();
+
+// Pairs per lane per pass of the FP64 Phi assembly (independent Heron chains in flight); 3 and
+// 4 measured slower than 2 (register pressure at the 128-register budget).
+#ifndef RBFFD_PHI_NP
+#define RBFFD_PHI_NP 2
+#endif
+
+// One pass of the packed FP64 Phi: strictly lower pairs t0 + lane + 32 u, u < NP, stored at
+// tri_off(i) + j = t + i.
+template <int NP>
 __device__ __forceinline__ void phi_pair_pass(const double *xs, int n, int p, double *phiP, int t0, int lane)
 {
     const int npairs = n * (n - 1) / 2;
-    const int t = t0 + lane;
-    if (t >= npairs) return;
-    const int t2 = t + 32;
-    const bool two = t2 < npairs;
-    int i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)t)) * 0.5f);
-    if ((i * (i - 1)) / 2 > t) i--;
-    if (((i + 1) * i) / 2 <= t) i++;
-    const int j = t - (i * (i - 1)) / 2;
-    const int tt = two ? t2 : t;
-    int i2 = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)tt)) * 0.5f);
-    if ((i2 * (i2 - 1)) / 2 > tt) i2--;
-    if (((i2 + 1) * i2) / 2 <= tt) i2++;
-    const int j2 = tt - (i2 * (i2 - 1)) / 2;
-    const double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
-    const double dx2 = xs[2 * i2] - xs[2 * j2], dy2 = xs[2 * i2 + 1] - xs[2 * j2 + 1];
-    const double v = phi64_nr(fma(dx, dx, dy * dy), p);
-    const double v2 = phi64_nr(fma(dx2, dx2, dy2 * dy2), p);
-    phiP[t + i] = v;
-    if (two) phiP[tt + i2] = v2;
+    double v[NP];
+    int ti[NP];
+#pragma unroll
+    for (int u = 0; u < NP; u++) {
+        const int t = t0 + lane + 32 * u;
+        const int ij = g_pair_table.ij[t < npairs ? t : 0];
+        const int i = ij >> 8, j = ij & 0xff;
+        const double dx = xs[2 * i] - xs[2 * j], dy = xs[2 * i + 1] - xs[2 * j + 1];
+        v[u] = phi64_nr(fma(dx, dx, dy * dy), p);
+        ti[u] = t < npairs ? t + i : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < NP; u++)
+        if (ti[u] >= 0) phiP[ti[u]] = v[u];
 }
 
-// The packed FP64 Phi (two pairs per lane per pass), its zero diagonal and the FP64 P rows.
+// The packed FP64 Phi, its zero diagonal and the FP64 P rows.
 __device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
                                                     double *P, int lane)
 {
-    const int npass = (n * (n - 1) / 2 + 63) / 64;
-    for (int q = 0; q < npass; q++) phi_pair_pass(xs, n, p, phiP, 64 * q, lane);
+    constexpr int NP = RBFFD_PHI_NP;
+    const int npass = (n * (n - 1) / 2 + 32 * NP - 1) / (32 * NP);
+    for (int q = 0; q < npass; q++) phi_pair_pass<NP>(xs, n, p, phiP, 32 * NP * q, lane);
     for (int i = lane; i < n; i += 32) {
         phiP[tri_off(i) + i] = 0.0;
         monomial_row<double>(xs[2 * i], xs[2 * i + 1], deg, P + i * m, 1);
