@@ -435,6 +435,26 @@ def test_errors(pkg, gpu):
     assert np.allclose(E.toarray(), np.eye(len(X)), atol=1e-10)
 
 
+def test_errors_closure_and_least_squares(pkg, gpu):
+    """Argument errors of the closure and CGLS entry points are EINVAL; a ghost block that is
+    exactly singular (a ghost no boundary row uses) is ESINGULAR; the handle stays usable."""
+    X, cls, s, B, G = _ghost_problem(pkg)
+    with s:
+        with pytest.raises(ValueError):
+            pkg.GhostClosure(s, "Dx", B[2], G[2][:-1])  # one ghost per boundary node
+        with pytest.raises(pkg.RbffdError) as e:
+            pkg.GhostClosure(s, "Dx", B[2], np.full(len(B[2]), len(X) + 5))  # out of range
+        assert e.value.code == 1
+        far = np.nonzero(cls == 0)[0][: len(B[2])]  # interior nodes: no boundary row of b = 2 uses them
+        with pytest.raises(pkg.RbffdError) as e:
+            pkg.GhostClosure(s, "Dx", B[2], far)
+        assert e.value.code == 3
+        with pytest.raises(ValueError):
+            s.lsq_cgls(np.zeros((1, s.rows)), np.zeros(s.rows))  # one coefficient row per operator
+        with pkg.GhostClosure(s, "Dx", B[2], G[2]):
+            pass
+
+
 @pytest.mark.parametrize("F", [2, 5, 64])
 @pytest.mark.parametrize("dtype,tol", [("f64", 1e-10), ("f32", 2e-5)])
 def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol, F):
