@@ -418,10 +418,38 @@ struct TopK {
     }
 };
 
-// Sweep the candidate segments [sa, sa+sl) held by lanes 0..nseg-1.
+// Exact FP64 keys of the queued candidates queue[0..cnt) (one per lane) and their insertion.
+template <int KS>
+__device__ __forceinline__ void take_queued(const GridDev &g, TopK<KS> &tk, const int64_t *queue, int cnt, double qx,
+                                            double qy, int lane)
+{
+    unsigned long long cd = KEY_INF;
+    int ci = INT_MAX;
+    if (lane < cnt) {
+        const int64_t t = queue[lane];
+        const double2 p = g.pts[t];
+        const double dx = __dsub_rn(qx, p.x), dy = __dsub_rn(qy, p.y);
+        cd = (unsigned long long)__double_as_longlong(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+        ci = g.ids[t];
+    }
+    unsigned m = __ballot_sync(RBFFD_FULL, key_less(cd, ci, tk.kd, tk.ki));
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const unsigned long long sd = __shfl_sync(RBFFD_FULL, cd, src);
+        const int si = __shfl_sync(RBFFD_FULL, ci, src);
+        if (key_less(sd, si, tk.kd, tk.ki)) tk.insert(sd, si, lane);
+    }
+}
+
+// Sweep the candidate segments [sa, sa+sl) held by lanes 0..nseg-1.  Candidates are screened
+// in FP32 against the current k-th distance (a bound that covers the conversions and FP32
+// rounding, so no candidate that can enter is dropped); the survivors are queued and their
+// exact FP64 distances computed 32 at a time, so the FP64 work (GB300: 1/64 rate) scales with
+// the survivors instead of all candidates.  The exact keys, and so the result, are unchanged.
 template <int KS>
 __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, int nseg, int64_t sa, int sl,
-                                               double qx, double qy, int cq, int lane)
+                                               double qx, double qy, int cq, int64_t *queue, int lane)
 {
     // exclusive offsets of the segments
     int inc = sl;
@@ -432,6 +460,8 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
     }
     int off = inc - sl;
     int total = __shfl_sync(RBFFD_FULL, inc, 31);
+    const float qx32 = f64_to_f32(qx), qy32 = f64_to_f32(qy);
+    int qn = 0;  // queued survivors (warp uniform), < 32 between batches
     for (int base = 0; base < total; base += 32) {
         int pos = base + lane;
         // find my segment: the last segment whose offset <= pos
@@ -442,27 +472,41 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
         }
         int64_t a = __shfl_sync(RBFFD_FULL, sa, seg);
         int os = __shfl_sync(RBFFD_FULL, off, seg);
-        unsigned long long cd = KEY_INF;
-        int ci = INT_MAX;
+        // float upper bound of the current k-th squared distance (inf while the list fills)
+        const float kd32 = f64_to_f32(__longlong_as_double((long long)tk.kd)) * (1.0f + 0x1p-20f);
+        bool pass = false;
+        int64_t t = 0;
         if (pos < total) {
-            int64_t t = a + (pos - os);
+            t = a + (pos - os);
             int cc = g.cls ? g.cls[t] : 0;
             if (class_allowed(cq, cc)) {
-                double2 p = g.pts[t];
-                double dx = __dsub_rn(qx, p.x), dy = __dsub_rn(qy, p.y);
-                cd = (unsigned long long)__double_as_longlong(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                ci = g.ids[t];
+                const double2 p = g.pts[t];
+                // the truncating conversions err by < 2^-23 relative, the FP32 difference and
+                // square sum by < 2^-24 each: err bounds |d32 - d2|
+                const float px = f64_to_f32(p.x), py = f64_to_f32(p.y);
+                const float dx = qx32 - px, dy = qy32 - py;
+                const float ex = 0x1p-22f * (fabsf(qx32) + fabsf(px)), ey = 0x1p-22f * (fabsf(qy32) + fabsf(py));
+                const float d32 = fmaf(dx, dx, dy * dy);
+                const float err = ex * (2.0f * fabsf(dx) + ex) + ey * (2.0f * fabsf(dy) + ey) + 0x1p-21f * d32;
+                pass = !(d32 - err > kd32);  // NaN (coordinates beyond the float range) keeps it
             }
         }
-        unsigned m = __ballot_sync(RBFFD_FULL, key_less(cd, ci, tk.kd, tk.ki));
-        while (m) {
-            int src = __ffs(m) - 1;
-            m &= m - 1;
-            unsigned long long sd = __shfl_sync(RBFFD_FULL, cd, src);
-            int si = __shfl_sync(RBFFD_FULL, ci, src);
-            if (key_less(sd, si, tk.kd, tk.ki)) tk.insert(sd, si, lane);
+        const unsigned m = __ballot_sync(RBFFD_FULL, pass);
+        if (pass) queue[qn + __popc(m & ((1u << lane) - 1u))] = t;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+            take_queued<KS>(g, tk, queue, 32, qx, qy, lane);
+            const int rest = qn - 32;
+            const int64_t mv = lane < rest ? queue[32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) queue[lane] = mv;
+            qn = rest;
+            __syncwarp();
         }
     }
+    if (qn > 0) take_queued<KS>(g, tk, queue, qn, qx, qy, lane);
+    __syncwarp();
 }
 
 template <int KS>
@@ -479,6 +523,8 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    __shared__ int64_t queue_all[8][64];  // survivors of the FP32 screen, per warp
+    int64_t *queue = queue_all[threadIdx.x >> 5];
     for (int64_t q = warp; q < nq; q += nwarps) {
         // node queries: query q is node q_node[q] (or q) of the set; its coordinates, class,
         // stencil size and output row are taken by node id.  Point queries: Q[q], class 0.
@@ -507,7 +553,7 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
                         sa = g.start[c0];
                         sl = g.start[c1] - g.start[c0];
                     }
-                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, lane);
+                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane);
                 }
             } else {
                 // ring: bottom row, top row (full width), then left/right cells of the middle rows
@@ -535,7 +581,7 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
                             sl = g.start[c1] - g.start[c0];
                         }
                     }
-                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, lane);
+                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane);
                 }
             }
             // distance from q to the unsearched cells
