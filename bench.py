@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-phases", action="store_true", help="reference arm: skip the full-size CPU phase times")
     ap.add_argument("--workload", default="collocated", choices=["collocated", "uneven", "rk4"],
                     help="collocated: the headline line; uneven: mixed stencil sizes with boundary and ghost "
                          "classes (2,097,152 nodes); rk4: advection-diffusion-hyperviscosity RK4 on 2048^2 nodes")
@@ -169,6 +170,39 @@ def cpu_sample_rate(X, target_s, nthreads=0, seed=0):
         size = min(len(X), int(size * max(2.0, target_s / max(dt, 1e-3))))
 
 
+def cpu_phases(X, solve_rate, seed=11):
+    """Per-phase CPU times of the oracle at the full node count: kNN of every node (all
+    threads), the weight solves (extrapolated from the sampled rate), sparse(I, J, V) of one
+    operator, and one SpMV both as single-threaded CSC (Julia's `*`) and as threaded row form."""
+    from oracle import oracle as orc
+
+    N, n = len(X), WORKLOAD["n"]
+    t0 = time.perf_counter()
+    cols, _ = orc.knn(X, X, n)
+    knn_ms = 1e3 * (time.perf_counter() - t0)
+    W = np.random.default_rng(seed).standard_normal((N, n))
+    t0 = time.perf_counter()
+    colptr, rowval, nzval = orc.to_csc(N, N, cols, W)
+    csc_ms = 1e3 * (time.perf_counter() - t0)
+    x = np.random.default_rng(seed + 1).standard_normal(N)
+    t0 = time.perf_counter()
+    y_csc = orc.spmv_csc(N, colptr, rowval, nzval, x)
+    spmv_csc_ms = 1e3 * (time.perf_counter() - t0)
+    orc.spmv_rows(cols, W, x)
+    t0 = time.perf_counter()
+    y_rows = orc.spmv_rows(cols, W, x)
+    spmv_rows_ms = 1e3 * (time.perf_counter() - t0)
+    if not np.allclose(y_csc, y_rows, rtol=1e-12, atol=1e-12):
+        raise RuntimeError("CPU SpMV forms disagree")
+    return {
+        "knn_all_nodes": knn_ms,
+        "solves_all_nodes_extrapolated": 1e3 * N / solve_rate,
+        "csc_build_per_op": csc_ms,
+        "spmv_csc_1_thread": spmv_csc_ms,
+        "spmv_rows_all_threads": spmv_rows_ms,
+    }
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if ws > 1 and rank != 0:
@@ -189,6 +223,7 @@ def run_reference(args):
             times.append(time.perf_counter() - t0)
     ms = 1e3 * float(np.mean(times))
     value = size / (ms * 1e-3)
+    phases = cpu_phases(X, value) if not args.no_cpu_phases else None
     sample = (f"{size} random rows of the {len(X)}-node workload per step (stencils, explicit "
               f"inverse of the 40x40 system, weights of Dx/Dy/Lap), C oracle port, {cores} threads")
     print(json.dumps({
@@ -206,7 +241,8 @@ def run_reference(args):
         "dtype": "f64",
         "data": "synthetic (seeded jittered grid)",
         "config": {"workload": "1024x1024 jittered nodes, p=3, deg=3, k=30, ops Dx,Dy,Lap", "rows_per_step": size},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
+                         "phases_ms_full_size": phases},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
