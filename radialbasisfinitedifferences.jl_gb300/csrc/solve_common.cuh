@@ -145,7 +145,10 @@ __device__ __forceinline__ double phi64_nr(double r2, int p)
         const double rt = sqrt_nr(r2, y0);
         v *= rt;
     }
-    return r2 >= DBL_MIN ? v : 0.0;  // r^p of a subnormal r^2 underflows to 0 in FP64
+    // r^p of a subnormal r^2 underflows to 0 in FP64.  r2 >= +0, so r2 >= DBL_MIN exactly when
+    // its high word (sign 0) reaches the smallest normal exponent: an integer compare instead
+    // of an FP64 one.
+    return __double2hiint(r2) >= 0x00100000 ? v : 0.0;
 }
 
 // phi = r^p from r^2 (odd p: r^(p-1) * r; even p: (r^2)^(p/2)).
