@@ -28,6 +28,7 @@
 #include <type_traits>
 
 #include "solve_common.cuh"
+#include "phi_fixed.cuh"
 
 namespace {
 
@@ -119,6 +120,8 @@ __host__ __device__ inline SchurLayout make_schur_layout(int SP, int SM, int max
     u += al16(sizeof(float) * max_m * n4);
     L.Sm = u;
     u += al16(sizeof(float) * max_m * max_m);
+    // the fixed-point coordinates of the Phi assembly (after the setup arrays are dead)
+    if (u < L.x32 + al16(sizeof(longlong2) * max_n)) u = L.x32 + al16(sizeof(longlong2) * max_n);
     // union: refinement arrays
     size_t v = o;
     L.B = v;
@@ -702,13 +705,54 @@ __device__ __forceinline__ void phi_pair_pass(const double *xs, int n, int p, do
         if (ti[u] >= 0) phiP[ti[u]] = v[u];
 }
 
-// The packed FP64 Phi, its zero diagonal and the FP64 P rows.
+// One pass of the packed Phi for odd p >= 3 from 61-bit fixed-point coordinates xf (no FP64
+// instruction for p = 3; r^(p-3) as FP64 products of r^2 otherwise).
+template <int NP>
+__device__ __forceinline__ void phi_pair_pass_fx(const longlong2 *xf, int n, int p, double *phiP, int t0, int lane)
+{
+    const int npairs = n * (n - 1) / 2;
+    double v[NP];
+    int ti[NP];
+#pragma unroll
+    for (int u = 0; u < NP; u++) {
+        const int t = t0 + lane + 32 * u;
+        const int ij = g_pair_table.ij[t < npairs ? t : 0];
+        const int i = ij >> 8, j = ij & 0xff;
+        const longlong2 a = xf[i], b = xf[j];
+        double r2 = 0.0;
+        double f = rbffd_fx::r3_fixed(a.x, a.y, b.x, b.y, p > 3 ? &r2 : nullptr);
+        for (int e = 3; e < p; e += 2) f *= r2;
+        v[u] = f;
+        ti[u] = t < npairs ? t + i : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < NP; u++)
+        if (ti[u] >= 0) phiP[ti[u]] = v[u];
+}
+
+// The packed FP64 Phi, its zero diagonal and the FP64 P rows.  Odd p >= 3 with all scaled
+// coordinates below 2 in magnitude (every scaled stencil) takes the fixed-point pair routine;
+// xf (16 bytes per node) is free scratch at this point.
 __device__ __forceinline__ void assemble_phi_packed(const double *xs, int n, int m, int deg, int p, double *phiP,
-                                                    double *P, int lane)
+                                                    double *P, longlong2 *xf, int lane)
 {
     constexpr int NP = RBFFD_PHI_NP;
     const int npass = (n * (n - 1) / 2 + 32 * NP - 1) / (32 * NP);
-    for (int q = 0; q < npass; q++) phi_pair_pass<NP>(xs, n, p, phiP, 32 * NP * q, lane);
+    bool fx = (p & 1) && p >= 3;
+    if (fx) {
+        bool in_range = true;
+        for (int i = lane; i < n; i += 32)
+            in_range = in_range && rbffd_fx::fixed61_ok(xs[2 * i]) && rbffd_fx::fixed61_ok(xs[2 * i + 1]);
+        fx = __all_sync(RBFFD_FULL, in_range);
+    }
+    if (fx) {
+        for (int i = lane; i < n; i += 32)
+            xf[i] = make_longlong2(rbffd_fx::to_fixed61(xs[2 * i]), rbffd_fx::to_fixed61(xs[2 * i + 1]));
+        __syncwarp();
+        for (int q = 0; q < npass; q++) phi_pair_pass_fx<NP>(xf, n, p, phiP, 32 * NP * q, lane);
+    } else {
+        for (int q = 0; q < npass; q++) phi_pair_pass<NP>(xs, n, p, phiP, 32 * NP * q, lane);
+    }
     for (int i = lane; i < n; i += 32) {
         phiP[tri_off(i) + i] = 0.0;
         monomial_row<double>(xs[2 * i], xs[2 * i + 1], deg, P + i * m, 1);
@@ -812,6 +856,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
     float *prow = (float *)(base + L.prow);
     double *sc = (double *)(base + L.sc);
     float2 *x32 = (float2 *)(base + L.x32);
+    longlong2 *xf = (longlong2 *)(base + L.x32);
     float *P32 = (float *)(base + L.P32);
     float *Pp = (float *)(base + L.Pp);
     float *Sm = (float *)(base + L.Sm);
@@ -855,7 +900,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
         bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
         if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
         bool fallback = !ok;
-        if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, lane);
+        if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, xf, lane);
         int64_t r0, r1;
         system_rows(a, sys, j, r0, r1);
         int iters_max = 0;
