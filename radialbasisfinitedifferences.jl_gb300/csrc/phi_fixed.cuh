@@ -163,7 +163,7 @@ RBFFD_FX_HD int64_t to_fixed61(double x)
 // |x| < 2 (the precondition of to_fixed61), by the exponent field.
 RBFFD_FX_HD bool fixed61_ok(double x) { return (f64_bits(x) & 0x7ff0000000000000ull) < 0x4000000000000000ull; }
 
-// Round a positive 64-bit value v to 53 bits and return v 2^e2 as a double; v >= 2^52.
+// Round a 64-bit value v > 0 to 53 bits and return v 2^e2 as a double (normal range).
 RBFFD_FX_HD double u64_scaled_to_f64(uint64_t v, int e2)
 {
     const int lz = clz64(v);
