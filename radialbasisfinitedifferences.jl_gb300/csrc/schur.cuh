@@ -443,6 +443,48 @@ __device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int 
     __syncwarp();
 }
 
+// a = hi + lo with hi the float truncation of a and lo the float truncation of the remaining
+// 29 mantissa bits (|a - hi - lo| <= 2^-47 |a|), from the bit fields (integer pipe).
+__device__ __forceinline__ void split_f64(double a, float &hi, float &lo)
+{
+    hi = f64_to_f32(a);
+    const unsigned h = (unsigned)__double2hiint(a), l = (unsigned)__double2loint(a);
+    const int e = (int)((h >> 20) & 0x7ffu);
+    const unsigned rem = l & 0x1fffffffu;  // mantissa bits below the float's 23
+    // rem * 2^(e - 1075), exact in the integer-to-float conversion up to rounding of 29 -> 24 bits
+    const int ex = e - 1075 + 127;
+    const float scale = ex > 0 && ex < 255 ? __uint_as_float((unsigned)ex << 23) : 0.0f;
+    const float v = __uint2float_rz(rem) * scale;
+    lo = (h & 0x80000000u) ? -v : v;
+}
+
+// Exact sum s + e = a + b of two floats (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Double-float (hi, lo) + d, renormalised: the refinement's solution and residual vectors are
+// kept in this form (48 significant bits) so that their updates need no FP64 instruction.
+__device__ __forceinline__ float2 df_add(float2 x, float d)
+{
+    float s, e;
+    two_sum(x.x, d, s, e);
+    float hi, lo;
+    two_sum(s, e + x.y, hi, lo);
+    return make_float2(hi, lo);
+}
+
+// A double as a double-float pair (split_f64: |v - hi - lo| <= 2^-47 |v|).
+__device__ __forceinline__ float2 df_from_f64(double v)
+{
+    float hi, lo;
+    split_f64(v, hi, lo);
+    return make_float2(hi, lo);
+}
+
 // Phi lower triangle (with its zero diagonal) packed by rows: element (i, j <= i) at
 // i (i + 1) / 2 + j.
 __device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
@@ -503,12 +545,13 @@ __device__ __forceinline__ void residual_phi_rows(const double *phiP, const doub
     for (int u = 0; u < NE; u++)
         if (ee[u] < tot) {
             const double v = a0[u] + a1[u];
-            if (store_r) B[ee[u]] = v;
+            if (store_r) reinterpret_cast<float2 *>(B)[ee[u]] = df_from_f64(v);
             R32[ee[u]] = f64_to_f32(v);
         }
 }
 
-// R32 <- float(B - A X) (and B <- B - A X when store_r) with FP64 products, lane-per-element: ceil(n r / 32) lane-full passes
+// R32 <- float(B - A X) (and B <- B - A X as double-float pairs when store_r) with FP64
+// products, lane-per-element: ceil(n r / 32) lane-full passes
 // of n + m FMAs for the Phi rows (two passes interleaved per lane), one pass of n FMAs per 32
 // elements for the P' rows.  Phi is read from its packed lower triangle.
 __device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r,
@@ -531,25 +574,10 @@ __device__ __forceinline__ void residual_schur(const double *phiP, const double 
         }
         if (jj < n) a0 = fma(-P[jj * m + l], X[jj * r + q], a0);
         const double v = a0 + a1;
-        if (store_r) B[(n + l) * r + q] = v;
+        if (store_r) reinterpret_cast<float2 *>(B)[(n + l) * r + q] = df_from_f64(v);
         R32[(n + l) * r + q] = f64_to_f32(v);
     }
     __syncwarp();
-}
-
-// a = hi + lo with hi the float truncation of a and lo the float truncation of the remaining
-// 29 mantissa bits (|a - hi - lo| <= 2^-47 |a|), from the bit fields (integer pipe).
-__device__ __forceinline__ void split_f64(double a, float &hi, float &lo)
-{
-    hi = f64_to_f32(a);
-    const unsigned h = (unsigned)__double2hiint(a), l = (unsigned)__double2loint(a);
-    const int e = (int)((h >> 20) & 0x7ffu);
-    const unsigned rem = l & 0x1fffffffu;  // mantissa bits below the float's 23
-    // rem * 2^(e - 1075), exact in the integer-to-float conversion up to rounding of 29 -> 24 bits
-    const int ex = e - 1075 + 127;
-    const float scale = ex > 0 && ex < 255 ? __uint_as_float((unsigned)ex << 23) : 0.0f;
-    const float v = __uint2float_rz(rem) * scale;
-    lo = (h & 0x80000000u) ? -v : v;
 }
 
 // s_hi + s_lo += a * d for floats a, d: the product exactly (TwoProduct by FMA), the sum by
@@ -566,12 +594,12 @@ __device__ __forceinline__ void df_mac(float a, float d, float &s_hi, float &s_l
     s_lo += err + e;
 }
 
-// Residual after a correction, r_new = r_old - A d, without FP64 products: d (the last
+// Residual after a correction, r_new = r_old - A d, without FP64 instructions: d (the last
 // correction, R32) is a float vector, A = hi + lo splits exactly enough, A d is accumulated as
-// a double-float sum, and only r_old - (s_hi + s_lo) is formed in FP64 (two adds per element).
-// The error of A d is ~2^-44 |A||d| with |d| ~ 1e-5 |x|, far below FP64 rounding of |A||x|,
-// so the refinement converges as with an FP64 residual.  B holds r_old and receives r_new;
-// R32 receives float(r_new).  Phi rows lane-per-row (the split of Phi_ij shared by the row's
+// a double-float sum and subtracted from r_old, itself a double-float pair.  The error of
+// A d is ~2^-44 |A||d| with |d| ~ 1e-5 |x|, and the pair holds r_old to 2^-47 of its size
+// (~1e-5 |A||x|), both far below FP64 rounding of |A||x|, so the refinement converges as with
+// an FP64 residual.  B holds r_old as (hi, lo) pairs and receives r_new; R32 receives hi.  Phi rows lane-per-row (the split of Phi_ij shared by the row's
 // operators), P' rows lane-per-element.
 template <int SP, int SM, int RMAX>
 __device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, double *B,
@@ -642,9 +670,10 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
 #pragma unroll
             for (int q = 0; q < RMAX; q++) {
                 if (q < r) {
-                    const double v = (B[i * r + q] - f32_to_f64(sh[k][q])) - f32_to_f64(sl[k][q]);
-                    B[i * r + q] = v;
-                    R32[i * r + q] = f64_to_f32(v);
+                    float2 *b2 = reinterpret_cast<float2 *>(B) + i * r + q;
+                    const float2 v = df_add(df_add(*b2, -sh[k][q]), -sl[k][q]);
+                    *b2 = v;
+                    R32[i * r + q] = v.x;
                 }
             }
         }
@@ -654,9 +683,10 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
         const int e = lane + 32 * u;
         if (e < m * r) {
             const int idx = n * r + e;
-            const double v = (B[idx] - f32_to_f64(th[u])) - f32_to_f64(tl[u]);
-            B[idx] = v;
-            R32[idx] = f64_to_f32(v);
+            float2 *b2 = reinterpret_cast<float2 *>(B) + idx;
+            const float2 v = df_add(df_add(*b2, -th[u]), -tl[u]);
+            *b2 = v;
+            R32[idx] = v.x;
         }
     }
     __syncwarp();
@@ -836,6 +866,27 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
     __syncwarp();
 }
 
+// One output row from the double-float solution: hi + lo (exact in FP64), times the
+// operator's scale factor sx^a sy^b (sc, the same product write_row forms) when it is applied
+// after the solve.
+__device__ __forceinline__ void write_row_df(const SolveArgs &a, const OpTable &ops, int64_t row, const float2 *X2,
+                                             int n, const int *sid, const double *sc, int lane)
+{
+    const int64_t off = a.row_ptr[row - a.row_begin];
+    const int r = ops.nops;
+    for (int l = lane; l < n; l += 32) a.col[off + l] = sid[l];
+    for (int q = 0; q < r; q++) {
+        double *dst = a.val + (int64_t)q * a.nnz + off;
+        const bool ps = ops.op[q].post_scale;
+        const double f = sc[2 * q];
+        for (int l = lane; l < n; l += 32) {
+            const float2 x = X2[l * r + q];
+            const double v = f32_to_f64(x.x) + f32_to_f64(x.y);
+            dst[l] = ps ? f * v : v;
+        }
+    }
+}
+
 template <int SP, int SM, int RMAX>
 __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
 {
@@ -922,21 +973,31 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                     residual_df<SP, SM, RMAX>(phiP, P, n, m, r, B, R32, lane);
                 }
                 schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
+                // x0 is kept as FP64 for the FP64 first residual; from the first update on, x is
+                // a double-float pair in the same 8 bytes of each element.
                 unsigned dkey = 0u, xkey = 0u;
                 for (int e = lane; e < s * r; e += 32) {
                     const float d = R32[e];
-                    const double xv = it == 0 ? f32_to_f64(d) : X[e] + f32_to_f64(d);
-                    X[e] = xv;
+                    float xh;
+                    if (it == 0) {
+                        X[e] = f32_to_f64(d);
+                        xh = d;
+                    } else {
+                        float2 *x2 = reinterpret_cast<float2 *>(X) + e;
+                        const float2 v = df_add(it == 1 ? make_float2(f64_to_f32(X[e]), 0.0f) : *x2, d);
+                        *x2 = v;
+                        xh = v.x;
+                    }
                     if (e < n * r) {
                         dkey = max(dkey, __float_as_uint(d) & 0x7fffffffu);
-                        xkey = max(xkey, (unsigned)__double2hiint(xv) & 0x7fffffffu);
+                        xkey = max(xkey, __float_as_uint(xh) & 0x7fffffffu);
                     }
                 }
                 dkey = __reduce_max_sync(RBFFD_FULL, dkey);
                 xkey = __reduce_max_sync(RBFFD_FULL, xkey);
                 __syncwarp();
                 const float dmax = __uint_as_float(dkey);
-                const float xmax = f64_to_f32(__hiloint2double((int)xkey, 0));
+                const float xmax = __uint_as_float(xkey);
                 const float e_cur = xmax > 0.0f ? __fdividef(dmax, xmax) : 0.0f;
                 if (!(e_cur == e_cur) || isinf(e_cur)) break;
                 if (it >= 1) {
@@ -954,7 +1015,7 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                 break;
             }
             if (it > iters_max) iters_max = it;
-            write_row(a, ops, row, X, n, sid, sx, sy, lane);
+            write_row_df(a, ops, row, reinterpret_cast<const float2 *>(X), n, sid, sc, lane);
             __syncwarp();
         }
         if (lane == 0) {
