@@ -927,7 +927,7 @@ static int ensure_csc(rbffd_handle *h, rbffd_opset *s)
     CK(launch_csc_count(s->nnz, s->col, count, st));
     CK(scan_exclusive_i64(count, colstart, N, scratch, tb, st));
     CK(launch_csc_scatter(s->rows, s->row_ptr, s->col, s->row_begin, colstart, fill, rowval, perm, st));
-    CK(launch_csc_sort_segments(N, colstart, rowval, perm, st));
+    CK(launch_csc_sort_segments(N, colstart, rowval, perm, s->row_begin + s->rows, st));
     // Julia is 1-based
     CK(launch_add_i64(N + 1, colstart, 1, st));
     CK(launch_add_i64(s->nnz, rowval, 1, st));
@@ -1518,7 +1518,7 @@ struct EarlyCsc : PatternHook {
         CK(launch_csc_count(nnz, nbr, count, st));
         CK(scan_exclusive_i64(count, colstart, N, scratch, tb, st));
         CK(launch_csc_scatter(N, row_ptr, nbr, 0, colstart, fill, rowval, perm, st));
-        CK(launch_csc_sort_segments(N, colstart, rowval, perm, st));
+        CK(launch_csc_sort_segments(N, colstart, rowval, perm, N, st));
         CK(launch_add_i64(N + 1, colstart, 1, st));  // Julia is 1-based
         CK(launch_add_i64(nnz, rowval, 1, st));
         CK(cudaFreeAsync(count, st));
@@ -1567,18 +1567,26 @@ static int build_and_export(rbffd_handle *h, const rbffd_problem *pb, int unscal
         return rc;
     }
     if (ec.active) {
-        cudaStream_t st = h->stream;
+        // values in CSC order: each operator gathered into its own buffer on the main stream and
+        // downloaded on the side stream as soon as its gather is done, so that the copies of
+        // one operator overlap the gathers of the next
+        cudaStream_t st = h->stream, ss = h->side;
         double *buf = nullptr;
         cudaError_t e = cudaStreamWaitEvent(st, h->side_ev[1], 0);
-        if (e == cudaSuccess) e = cudaMallocAsync((void **)&buf, sizeof(double) * s->nnz, st);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&buf, sizeof(double) * s->nnz * s->nops, st);
         for (int q = 0; q < s->nops && e == cudaSuccess; q++) {
             if (!out[q].nzval) continue;
-            e = launch_gather_f64(s->nnz, ec.perm, s->val + (size_t)q * s->nnz, buf, st);
+            double *bq = buf + (size_t)q * s->nnz;
+            e = launch_gather_f64(s->nnz, ec.perm, s->val + (size_t)q * s->nnz, bq, st);
+            if (e == cudaSuccess) e = cudaEventRecord(h->side_ev[0], st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, h->side_ev[0], 0);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(out[q].nzval, buf, sizeof(double) * s->nnz, cudaMemcpyDeviceToHost, st);
+                e = cudaMemcpyAsync(out[q].nzval, bq, sizeof(double) * s->nnz, cudaMemcpyDeviceToHost, ss);
         }
+        cudaError_t e2 = cudaStreamSynchronize(ss);
+        if (e == cudaSuccess) e = e2;
         if (buf) cudaFreeAsync(buf, st);
-        cudaError_t e2 = cudaStreamSynchronize(st);
+        e2 = cudaStreamSynchronize(st);
         if (e == cudaSuccess) e = e2;
         rc = e == cudaSuccess ? RBFFD_OK : fail(h, RBFFD_ECUDA, std::string("csc export: ") + cudaGetErrorString(e));
     } else {

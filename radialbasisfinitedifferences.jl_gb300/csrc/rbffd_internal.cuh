@@ -235,8 +235,9 @@ cudaError_t launch_csc_count(int64_t nnz, const int32_t *col, int64_t *colcount,
 cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32_t *col,
                                int64_t row_begin, const int64_t *colstart, int64_t *fill,
                                int64_t *rowval, int64_t *perm, cudaStream_t st);
+// Sorts each column segment of (rowval, perm) by row; row_limit bounds the row ids (0-based).
 cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                     int64_t *perm, cudaStream_t st);
+                                     int64_t *perm, int64_t row_limit, cudaStream_t st);
 cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *src, double *dst,
                               cudaStream_t st);
 cudaError_t launch_add_i64(int64_t n, int64_t *a, int64_t v, cudaStream_t st);

@@ -700,7 +700,7 @@ __global__ void csc_scatter_kernel(int64_t rows, const int64_t *row_ptr, const i
 // with a smaller row (rows inside a column are distinct); segments longer than 256 fall back
 // to one lane's insertion sort.
 __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                int64_t *perm)
+                                int64_t *perm, bool keys32)
 {
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -709,7 +709,39 @@ __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t 
         int64_t a = colstart[c], b = colstart[c + 1];
         int len = (int)(b - a);
         if (len <= 1) continue;
-        if (len <= 256) {
+        if (keys32 && len <= 64) {
+            // The common case (a column of a kNN operator holds ~k rows): rank sort of two
+            // register slots with 32-bit keys.  Row ids within a column are distinct, and the
+            // padding key 0xffffffff exceeds every row id, so ranks are a permutation of [0, len).
+            const int t1 = lane + 32;
+            const int64_t r0 = lane < len ? rowval[a + lane] : 0, p0 = lane < len ? perm[a + lane] : 0;
+            const int64_t r1 = t1 < len ? rowval[a + t1] : 0, p1 = t1 < len ? perm[a + t1] : 0;
+            const unsigned k0 = lane < len ? (unsigned)r0 : 0xffffffffu, k1 = t1 < len ? (unsigned)r1 : 0xffffffffu;
+            int rk0 = 0, rk1 = 0;
+#pragma unroll 8
+            for (int src = 0; src < 32; src++) {
+                const unsigned o = __shfl_sync(RBFFD_FULL, k0, src);
+                rk0 += o < k0;
+                rk1 += o < k1;
+            }
+            if (len > 32) {
+#pragma unroll 8
+                for (int src = 0; src < 32; src++) {
+                    const unsigned o = __shfl_sync(RBFFD_FULL, k1, src);
+                    rk0 += o < k0;
+                    rk1 += o < k1;
+                }
+            }
+            __syncwarp();
+            if (lane < len) {
+                rowval[a + rk0] = r0;
+                perm[a + rk0] = p0;
+            }
+            if (t1 < len) {
+                rowval[a + rk1] = r1;
+                perm[a + rk1] = p1;
+            }
+        } else if (len <= 256) {
             int64_t rv[8], pv[8];
             int rk[8];
 #pragma unroll
@@ -999,9 +1031,10 @@ cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32
 }
 
 cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                     int64_t *perm, cudaStream_t st)
+                                     int64_t *perm, int64_t row_limit, cudaStream_t st)
 {
-    csc_sort_kernel<<<blocks_for(ncols * 32, 256), 256, 0, st>>>(ncols, colstart, rowval, perm);
+    const bool keys32 = row_limit < 0xffffffffll;  // row ids fit 32-bit keys below the padding key
+    csc_sort_kernel<<<blocks_for(ncols * 32, 256), 256, 0, st>>>(ncols, colstart, rowval, perm, keys32);
     return cudaGetLastError();
 }
 

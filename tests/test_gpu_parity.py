@@ -130,6 +130,26 @@ def test_generate_operator_csc_matches_sparse(pkg, orc, gpu):
         assert np.abs(A.data - nz).max() <= FP64_TOL * scale * 10
 
 
+@pytest.mark.parametrize("n", [20, 40, 80])
+def test_generate_operator_collocated_csc(pkg, orc, gpu, n):
+    """The collocated drop-in path (CSC pattern built before the solves, values gathered and
+    downloaded per operator) equals sparse(I, J, V) of the oracle.  n = 20, 40, 80 put the
+    columns in the sort's one-slot, two-slot and general (> 64 rows) cases."""
+    X, _ = grid(pkg, 30, seed=4)
+    p, deg = 3, 2
+    ops = ("Dx", "Lap")
+    mats = pkg.generate_operator(X, X, p, n, deg, ops=ops, precision="fp64")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    lens = np.diff(orc.to_csc(len(X), len(X), ref["cols"], ref["W"][0])[0])
+    assert lens.max() > (64 if n == 80 else 32 if n == 40 else 1)
+    for q, A in enumerate(mats):
+        cp, rv, nz = orc.to_csc(len(X), len(X), ref["cols"], ref["W"][q])
+        assert np.array_equal(A.indptr, cp - 1)
+        assert np.array_equal(A.indices, rv - 1)
+        scale = np.abs(ref["W"][q]).max()
+        assert np.abs(A.data - nz).max() <= FP64_TOL * scale * 10
+
+
 def test_unscaled_overload(pkg, orc, gpu):
     X, _ = grid(pkg, 32, seed=8)
     p, n, deg = 3, 15, 2
