@@ -247,6 +247,27 @@ def run_reference(args):
     }))
 
 
+def manufactured_errors(pkg, h):
+    """The 64x64 manufactured-solution case (p=3, deg 2, k=15): f = sin(2 pi x) cos(3 pi y)
+    applied through the device operators of both precisions (SELL SpMV); max error on the
+    interior nodes (|x - 1/2|, |y - 1/2| < 0.35) relative to the exact derivative's max."""
+    import torch
+
+    X, _, _ = pkg.nodesets.jittered_grid(64, seed=1)
+    f, fx, fy, lap = pkg.nodesets.manufactured(X)
+    inner = (np.abs(X - 0.5) < 0.35).all(1)
+    exact = {"Dx": fx, "Dy": fy, "Lap": lap}
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with pkg.OperatorSet(X, None, 3, 15, 2, ops=("Dx", "Dy", "Lap"), precision=prec, handle=h) as s:
+            fd = torch.tensor(f, device="cuda")
+            yd = torch.empty_like(fd)
+            for o, ex in exact.items():
+                y = s.spmv(o, fd, yd).cpu().numpy()
+                out[f"{prec}_{o}"] = float(np.abs(y - ex)[inner].max() / np.abs(ex).max())
+    return out
+
+
 def row_rel_err(a, b, n):
     """max over rows of ||a_i - b_i||_inf / ||b_i||_inf for row-major (rows, n) torch tensors."""
     import torch
@@ -436,6 +457,7 @@ def run_ours(args):
                "sample": f"{size} random rows of the {rows_per}-node workload (kNN, explicit inverse, Dx/Dy/Lap "
                          f"weights), C oracle port, {dt:.1f} s"}
 
+    manu = manufactured_errors(pkg, h)
     m = 10
     s_ = n + m
     # FP64 work of the mixed solve per system: the monomials of P, the right-hand sides, the
@@ -480,6 +502,7 @@ def run_ours(args):
             "max_row_rel_err_vs_oracle_2000_rows": err_oracle,
             "fallback_fraction": mixed_stats["n_fallback"] / max(1, mixed_stats["n_systems"]),
             "refine_hist": hist,
+            "manufactured_64x64_k15_deg2_rel_err": manu,
         },
         "fp64_form": {"value": rows_per * ws / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64,
                       "solve_kernel_ms": solve_ms_fp64},
