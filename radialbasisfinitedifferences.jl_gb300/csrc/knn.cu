@@ -534,9 +534,16 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
         int k = (node_query && kq) ? kq[node] : kuni;
         TopK<KS> tk;
         tk.init(k);
-        int cx = (int)floor((qp.x - g.x0) / g.cs), cy = (int)floor((qp.y - g.y0) / g.cs);
+        // The query's cell only seeds the search, so it is taken in FP32; the stopping test
+        // below uses the offset of q from the same cell's corner, fx = (qx - x0) - cx cs, formed
+        // once per query in FP64 (four FP64 instructions instead of a division per axis).
+        const double dqx = qp.x - g.x0, dqy = qp.y - g.y0;
+        const float cs32 = f64_to_f32(g.cs), ics32 = __frcp_rn(cs32);
+        int cx = __float2int_rd(f64_to_f32(dqx) * ics32), cy = __float2int_rd(f64_to_f32(dqy) * ics32);
         cx = cx < 0 ? 0 : (cx >= g.nx ? g.nx - 1 : cx);
         cy = cy < 0 ? 0 : (cy >= g.ny ? g.ny - 1 : cy);
+        const float fx = f64_to_f32(fma(-f32_to_f64((float)cx), g.cs, dqx));
+        const float fy = f64_to_f32(fma(-f32_to_f64((float)cy), g.cs, dqy));
         bool done = false;
         for (int R = r0; !done; R++) {
             // segments of this sweep: the full square at R = r0, then the ring at radius R
@@ -584,15 +591,21 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
                     sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane);
                 }
             }
-            // distance from q to the unsearched cells
-            double bound = CUDART_INF;
-            if (cx - R > 0) bound = fmin(bound, qp.x - (g.x0 + (cx - R) * g.cs));
-            if (cx + R < g.nx - 1) bound = fmin(bound, (g.x0 + (cx + R + 1) * g.cs) - qp.x);
-            if (cy - R > 0) bound = fmin(bound, qp.y - (g.y0 + (cy - R) * g.cs));
-            if (cy + R < g.ny - 1) bound = fmin(bound, (g.y0 + (cy + R + 1) * g.cs) - qp.y);
-            if (bound == CUDART_INF) done = true;
-            else if (bound > 0 && tk.kd < (unsigned long long)__double_as_longlong(bound * bound * (1.0 - 1e-12)))
-                done = true;
+            // distance from q to the unsearched cells: to the sides of the searched square
+            // [cx - R, cx + R] x [cy - R, cy + R] that are not the grid's edge, in FP32.  The
+            // terms carry a few FP32 roundings (relative 2^-22 at most) and the cell
+            // assignment of the grid build a relative 2^-50; the square is shrunk by 2^-18
+            // so that it stays a lower bound and the exact keys decide as before.
+            float bound = CUDART_INF_F;
+            if (cx - R > 0) bound = fminf(bound, fmaf((float)R, cs32, fx));
+            if (cx + R < g.nx - 1) bound = fminf(bound, fmaf((float)(R + 1), cs32, -fx));
+            if (cy - R > 0) bound = fminf(bound, fmaf((float)R, cs32, fy));
+            if (cy + R < g.ny - 1) bound = fminf(bound, fmaf((float)(R + 1), cs32, -fy));
+            if (bound == CUDART_INF_F) done = true;
+            else if (bound > 0.0f) {
+                const float b2 = bound * bound * (1.0f - 0x1p-18f);
+                done = tk.kd < (unsigned long long)__double_as_longlong(f32_to_f64(b2));
+            }
         }
         int64_t ob = out_ptr ? out_ptr[node] : node * (int64_t)k;
         bool short_list = !(tk.kd < KEY_INF);
