@@ -787,6 +787,9 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         } else {
             launches.push_back(a);
         }
+        unsigned long long *claim;
+        CK(tmp.zeros(&claim, launches.size()));
+        for (size_t i = 0; i < launches.size(); i++) launches[i].next_sys = claim + i;
         for (const SolveArgs &ab : launches) {
             cudaError_t e = launch_solve_mixed_reg(ab, table, ab.max_m, 4, h->num_sms, st);
             if (e == cudaErrorNotSupported) {
@@ -1500,6 +1503,8 @@ struct EarlyCsc : PatternHook {
 
     int build(rbffd_handle *h, int64_t N_, int n, const int64_t *row_ptr, const int32_t *nbr) override
     {
+        // on the main stream, ahead of the weight solves (their persistent grid would hold
+        // every SM until its end); only the download runs beside the solves
         cudaStream_t st = h->stream;
         N = N_;
         nnz = N_ * n;

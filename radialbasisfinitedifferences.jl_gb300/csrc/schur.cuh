@@ -927,7 +927,15 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
 
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t ts = gw; ts < a.nsys; ts += nw) {
+    // Systems are claimed from a counter when one is given (warps that start late -- behind
+    // kernels of another stream -- then simply take fewer), else by a fixed grid stride.
+    auto next = [&](int64_t cur) -> int64_t {
+        if (!a.next_sys) return cur + nw;
+        unsigned long long v = 0ull;
+        if (lane == 0) v = atomicAdd(a.next_sys, 1ull);
+        return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
+    };
+    for (int64_t ts = a.next_sys ? next(0) : gw; ts < a.nsys; ts = next(ts)) {
         const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
         const int j = a.sys_node[sys];
         const int n = a.n_node ? a.n_node[j] : a.n;
