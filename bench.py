@@ -57,7 +57,7 @@ WORKLOAD = dict(p=3, n=30, deg=3, ops=("Dx", "Dy", "Lap"))
 # DRAM traffic per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum):
 # the mixed solve on 512x512 nodes (262,144 systems; traffic is the gathered stencils and the
 # CSR output, so it scales with the systems) and the SELL SpMV on 1024x1024 nodes (31.46 M nnz).
-NCU_TRAFFIC = {"solve_bytes_per_system": (47.78e6 + 174.54e6) / 262144,
+NCU_TRAFFIC = {"solve_bytes_per_system": (46.59e6 + 174.67e6) / 262144,
                "spmv_bytes_per_nnz": (385.90e6 + 4.11e6) / 31457280}
 
 
