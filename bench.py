@@ -53,6 +53,13 @@ def parse():
 
 
 WORKLOAD = dict(p=3, n=30, deg=3, ops=("Dx", "Dy", "Lap"))
+METRIC = "weight solves/s at <=1e-9 rel err (FP32+refine vs FP64); stencil-apply HBM GB/s"
+
+
+def workload_name(nx):
+    """The headline workload as named in both arms' `config.workload`."""
+    return (f"{nx}x{nx} jittered nodes per GPU (h=1/{nx}, +-0.3h), PHS r^3, deg 3 (m=10), "
+            f"k=30 (s=40), ops Dx,Dy,Lap; step = grid+kNN+mixed solves+CSR + 1 SpMV per op")
 
 # DRAM traffic per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum):
 # the mixed solve on 512x512 nodes (262,144 systems; traffic is the gathered stencils and the
@@ -228,7 +235,7 @@ def run_reference(args):
               f"inverse of the 40x40 system, weights of Dx/Dy/Lap), C oracle port, {cores} threads")
     print(json.dumps({
         "impl": "reference",
-        "metric": "weight solves/s (N=1,048,576, k=30, deg 3, PHS r^3; Dx, Dy, Lap)",
+        "metric": METRIC,
         "value": value,
         "unit": "solves/s",
         "n_gpus": args.gpus,
@@ -240,7 +247,8 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded jittered grid)",
-        "config": {"workload": "1024x1024 jittered nodes, p=3, deg=3, k=30, ops Dx,Dy,Lap", "rows_per_step": size},
+        "config": {"workload": workload_name(args.nx), "rows_per_step": size,
+                   "parallelism": f"host cores x{cores}"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
                          "phases_ms_full_size": phases},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -473,7 +481,7 @@ def run_ours(args):
     hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800 GB/s"
     hbm = hbm or 6800.0
     out = {
-        "metric": "weight solves/s at <=1e-9 rel err (FP32+refine vs FP64); stencil-apply HBM GB/s",
+        "metric": METRIC,
         "value": value,
         "unit": "solves/s",
         "n_gpus": ws,
@@ -486,8 +494,7 @@ def run_ours(args):
         "dtype": "f32+f64",
         "data": "synthetic (seeded jittered grid, splitmix64)",
         "config": {
-            "workload": f"{args.nx}x{args.nx} jittered nodes per GPU (h=1/{args.nx}, +-0.3h), PHS r^3, deg 3 (m=10), "
-                        f"k=30 (s=40), ops Dx,Dy,Lap; step = grid+kNN+mixed solves+CSR + 1 SpMV per op",
+            "workload": workload_name(args.nx),
             "rows_per_gpu": rows_per,
             "l2": "flushed (256 MB write) before every step",
             "parallelism": f"row shards x{ws}" if ws > 1 else "single GPU",
