@@ -4,7 +4,10 @@
 // (src/generate_operator.jl:43-47) and the boundary-masked searches of calculateneighbors
 // (src/calculateneighbors.jl:16-42, :83-94).  Squared distances are rounded exactly as
 // dx*dx + dy*dy with two roundings and no FMA, and candidates are ordered by (d^2, id), so
-// the selected index sets are bit-identical to the CPU oracle's.
+// the selected index sets are bit-identical to the CPU oracle's.  Only candidates that pass an
+// FP32 screen against the current k-th distance get that exact FP64 distance, and the ring
+// search stops on an FP32 lower bound of the distance to the unsearched cells; both are
+// conservative, so the exact keys alone decide the result.
 #include <float.h>
 #include <limits.h>
 #include <math_constants.h>

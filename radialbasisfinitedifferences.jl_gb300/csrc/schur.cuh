@@ -1,5 +1,5 @@
 // Mixed-precision weight solves: FP32 preconditioner built from the Schur complement of the
-// saddle system, FP64 residuals, iterative refinement.  One warp per local system.
+// saddle system, an FP64 first residual, iterative refinement.  One warp per local system.
 //
 // The local system of src/generate_operator.jl (rbfblock/polynomialblock) is
 //   A = [Phi P; P' 0],  Phi_ij = phi(|x_i - x_j|) (n x n),  P_il = monomial l at x_i (n x m).
@@ -11,10 +11,13 @@
 // A correction A^-1 [r1; r2] = [w; lambda] is then
 //   lambda = Sinv (r2 - G' r1),   w = Phi^-1 r1 - G lambda,
 // i.e. one register matvec plus three short shared-memory matvecs.  Refinement x += A^-1 (b - A x)
-// runs with FP64 residuals (Phi packed as its lower triangle, P, x and b in FP64) until the
-// estimated relative error of the weights rho * |dx| / |x| is below refine_tol; a system that
-// stalls (rho > 1/2), meets a zero pivot or produces a non-finite value goes to the FP64
-// fallback queue, as in the shared-memory mixed kernel of weights.cu.
+// keeps Phi (packed as its lower triangle) and P in FP64; the pairwise Phi = r^p comes from exact
+// fixed-point integer arithmetic (phi_fixed.cuh).  The first residual b - A x0 is formed with
+// FP64 products; from then on x and the residual are double-float pairs and each new residual
+// r - A d is a double-float FP32 dot product.  Refinement stops when the estimated relative
+// error of the weights rho * |dx| / |x| is below refine_tol; a system that stalls (rho > 1/2),
+// meets a zero pivot or produces a non-finite value goes to the FP64 fallback queue, as in the
+// shared-memory mixed kernel of weights.cu.  Warps claim systems from a counter.
 //
 // FP64 instructions are the scarce resource (1/64 of the FP32 rate), so every FP64 instruction
 // works on lane-parallel data, conversions between float and double use the integer pipe, and
