@@ -1075,3 +1075,8 @@ cudaError_t launch_schur_sp32(const SolveArgs &a, const OpTable &ops, int SM, in
 cudaError_t launch_schur_sp64(const SolveArgs &a, const OpTable &ops, int SM, int RMAX, int wpb, int num_sms,
                               cudaStream_t st);
 size_t schur_smem_per_warp(int SP, int SM, int max_n, int max_m, int nops);
+// The four 64-node instantiations, one per translation unit (weights_reg64_m<SM>_r<RMAX>.cu).
+cudaError_t launch_schur_64_16_4(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);
+cudaError_t launch_schur_64_16_8(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);
+cudaError_t launch_schur_64_32_4(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);
+cudaError_t launch_schur_64_32_8(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);

@@ -1,0 +1,8 @@
+// Schur-complement mixed solve (schur.cuh) for stencils of 33..64 nodes with at most 16
+// monomials and at most 8 operators (one instantiation per translation unit).
+#include "schur.cuh"
+
+cudaError_t launch_schur_64_16_8(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st)
+{
+    return launch_schur<64, 16, 8>(a, ops, wpb, num_sms, st);
+}
