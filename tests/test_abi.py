@@ -27,6 +27,24 @@ def test_library_builds_and_exports_header(pkg):
     assert L.rbffd_version() == 1
 
 
+def test_every_translation_unit_is_built(pkg):
+    """Every CUDA source of csrc/ is compiled into the library, and the library leaves no
+    symbol of its own unresolved (a shared library links even when one is missing)."""
+    import importlib
+    import subprocess
+
+    b = importlib.import_module(pkg.__name__ + "._build")
+    on_disk = sorted(f for f in os.listdir(b.CSRC) if f.endswith(".cu"))
+    assert sorted(b.SOURCES) == on_disk
+    path = pkg.build()
+    try:
+        out = subprocess.run(["nm", "-u", "-C", path], capture_output=True, text=True, check=True).stdout
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("nm not available")
+    own = [ln for ln in out.splitlines() if re.search(r"\b(rbffd_|launch_|solve_|schur_)", ln)]
+    assert not own, own
+
+
 def test_no_cpu_fallback_without_gpu(pkg):
     import torch
 
