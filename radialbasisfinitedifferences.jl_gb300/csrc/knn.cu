@@ -226,7 +226,8 @@ __global__ void bbox_final(const double *partial, int nb, double *out)
 cudaError_t launch_bbox(const double2 *X, int64_t N, double *partial, int nblocks, double *out,
                         int *out_bad, cudaStream_t st)
 {
-    cudaMemsetAsync(out_bad, 0, sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(out_bad, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
     bbox_partial<<<nblocks, 256, 0, st>>>(X, N, partial, out_bad);
     bbox_final<<<1, 32, 0, st>>>(partial, nblocks, out);
     return cudaGetLastError();
@@ -319,7 +320,8 @@ cudaError_t launch_grid_scatter(const double2 *X, const int32_t *cls, int64_t N,
 {
     int nb = (int)((N + 255) / 256);
     if (nb > 65535) nb = 65535;
-    cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncell, st);
+    cudaError_t e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * ncell, st);
+    if (e != cudaSuccess) return e;
     grid_scatter_kernel<<<nb, 256, 0, st>>>(X, cls, N, cell_of, cell_start64, fill, pts, ids,
                                             gcls);
     int nc = (int)((ncell + 1 + 255) / 256);
@@ -596,18 +598,26 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
             }
             // distance from q to the unsearched cells: to the sides of the searched square
             // [cx - R, cx + R] x [cy - R, cy + R] that are not the grid's edge, in FP32.  The
-            // terms carry a few FP32 roundings (relative 2^-22 at most) and the cell
-            // assignment of the grid build a relative 2^-50; the square is shrunk by 2^-18
-            // so that it stays a lower bound and the exact keys decide as before.
+            // error is absolute, not relative to the bound: cs32 and fx are truncations of
+            // FP64 values (each off by up to 2^-23 of its size), and a side term is small only
+            // when |fx| is close to R cs or (R + 1) cs, so the term can exceed the true
+            // distance by up to ~2^-22 (R + 1) cs however small it is.  2^-20 (R + 1) cs32 is
+            // taken off every bound before the test (it covers that error with room for the
+            // cell assignment of the grid build, relative 2^-50), and the square of what is
+            // left is shrunk by 2^-18 for the FP32 roundings of the last FMA and the square:
+            // a lower bound, so the exact keys decide.
             float bound = CUDART_INF_F;
             if (cx - R > 0) bound = fminf(bound, fmaf((float)R, cs32, fx));
             if (cx + R < g.nx - 1) bound = fminf(bound, fmaf((float)(R + 1), cs32, -fx));
             if (cy - R > 0) bound = fminf(bound, fmaf((float)R, cs32, fy));
             if (cy + R < g.ny - 1) bound = fminf(bound, fmaf((float)(R + 1), cs32, -fy));
             if (bound == CUDART_INF_F) done = true;
-            else if (bound > 0.0f) {
-                const float b2 = bound * bound * (1.0f - 0x1p-18f);
-                done = tk.kd < (unsigned long long)__double_as_longlong(f32_to_f64(b2));
+            else {
+                const float safe = fmaf(-0x1p-20f * (float)(R + 1), cs32, bound);
+                if (safe > 0.0f) {
+                    const float b2 = safe * safe * (1.0f - 0x1p-18f);
+                    done = tk.kd < (unsigned long long)__double_as_longlong(f32_to_f64(b2));
+                }
             }
         }
         int64_t ob = out_ptr ? out_ptr[node] : node * (int64_t)k;

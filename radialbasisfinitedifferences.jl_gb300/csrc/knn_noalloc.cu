@@ -14,6 +14,12 @@
 // Host code may not use the array's name as a device address (it is a host-side stand-in),
 // so the first call on each device, with that device current, looks the address up with
 // cudaGetSymbolAddress and caches it; make that first call before any stream capture.
+// Under CUDA's default lazy module loading the array is only placed in device memory when
+// this translation unit's module is first loaded on a device -- by that first call's
+// cudaGetSymbolAddress (at library load instead with CUDA_MODULE_LOADING=EAGER).  That first
+// call can therefore itself need the array's 5 MiB of free device memory, and returns
+// RBFFD_ECUDA if the device has none left: make it before the caller's allocator reserves
+// the device's memory.  Later calls need no device memory at all.
 // Every call reuses the same array and leaves its contents behind; everything that must
 // start at zero is cleared by the call itself.  Calls that overlap on the GPU (two streams,
 // two host threads) race on the array and must be serialised by the caller.

@@ -5,7 +5,7 @@ read Tominec's fitted node sets and index sets from CSV files under test/data/.
 This script converts exactly those files, unmodified, into one compressed .npz so
 that the parity tests can run where the reference checkout is absent.
 
-Usage:  python tests/golden/make_golden.py [path/to/RadialBasisFiniteDifferences.jl]
+Usage:  python tests/golden/make_golden.py path/to/RadialBasisFiniteDifferences.jl
 """
 import os
 import sys
@@ -38,4 +38,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py path/to/RadialBasisFiniteDifferences.jl (the reference checkout)")
+    main(sys.argv[1])

@@ -1,7 +1,12 @@
-"""Multi-rank path on CPU (gloo, world size 2): the weight solves shard by evaluation rows
-with no data-path collective; each rank builds rows [rank*R, (rank+1)*R) of one global node
-set, and the gathered shards equal the single-rank operator.  Timing is reduced with a max
-over ranks, as bench.py does under torchrun."""
+"""Shard arithmetic of the multi-rank path, on CPU (gloo, world size 2).
+
+The weight solves shard by evaluation rows with no data-path collective.  This test checks
+the host-side row partition that bench.py uses under torchrun (bench.node_set /
+bench.shard_rows: rank r owns rows [r*R, (r+1)*R) of one global node set) and the max-over-
+ranks timing reduction.  Each rank computes its shard with the CPU oracle -- not with
+librbffd, which needs a GPU -- and the gathered shards must equal the single-rank operator.
+The library's own row-range interface (rbffd_problem.row_begin/row_end) is checked on the
+GPU by test_gpu_parity.py::test_row_range_shards."""
 import os
 import socket
 
