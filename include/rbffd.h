@@ -133,6 +133,12 @@ int rbffd_create(const rbffd_options *opt, rbffd_handle **out);
 void rbffd_destroy(rbffd_handle *h);
 /* Text of the last error on this handle (never NULL). */
 const char *rbffd_last_error(const rbffd_handle *h);
+/* The weight-solve autotuner's choices on this handle, one line per shape class of local
+   systems seen so far ("mixed n<=30 m<=10 ops=3 p=3: schur x4 warps (timed on ... systems:
+   candidate times)"); classes too small to time get a heuristic choice and no line.  The text
+   stays valid until the next call on the handle.  No reference counterpart (the reference
+   runs the solves in a Threads.@threads loop, src/generate_operator.jl:55,89). */
+const char *rbffd_autotune_report(const rbffd_handle *h);
 /* The handle's cudaStream_t, as void*. */
 void *rbffd_stream(rbffd_handle *h);
 int rbffd_synchronize(rbffd_handle *h);
@@ -284,8 +290,12 @@ int rbffd_lsq_cgls(rbffd_handle *h, rbffd_opset *s, const double *coef, const do
  * Scratch lives in one static device array of RBFFD_NOALLOC_SCRATCH_BYTES per GPU, held
  * until the process exits; N above RBFFD_NOALLOC_MAX_NODES is rejected with RBFFD_EINVAL
  * (message in rbffd_last_error(NULL)).  The first call on each device looks the array's
- * address up (make it before any stream capture).  Calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.
+ * address up (make it before any stream capture).  With CUDA's default lazy module loading
+ * that first call is also when the array is placed in device memory, so it needs 5 MiB of
+ * free device memory (RBFFD_ECUDA if there is none; CUDA_MODULE_LOADING=EAGER places it at
+ * library load instead): make it before the caller's allocator reserves the device's
+ * memory.  Calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.
  * ------------------------------------------------------------------------------ */
 #define RBFFD_NOALLOC_MAX_NODES 65536
 #define RBFFD_NOALLOC_SCRATCH_BYTES (5u << 20)

@@ -21,6 +21,7 @@ EXPORTED = [
     "rbffd_create",
     "rbffd_destroy",
     "rbffd_last_error",
+    "rbffd_autotune_report",
     "rbffd_stream",
     "rbffd_synchronize",
     "rbffd_generate_operator",
@@ -149,6 +150,7 @@ def load(build_if_missing=False):
         "rbffd_create": ([P, P], i32),
         "rbffd_destroy": ([P], None),
         "rbffd_last_error": ([P], ctypes.c_char_p),
+        "rbffd_autotune_report": ([P], ctypes.c_char_p),
         "rbffd_stream": ([P], P),
         "rbffd_synchronize": ([P], i32),
         "rbffd_generate_operator": ([P, P, i64, P, i64, i32, i32, i32, P, u32, i32, P, P], i32),

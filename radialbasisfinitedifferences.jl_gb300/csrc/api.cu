@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "rbffd_internal.cuh"
+#include "tune.cuh"
 
 #define RBFFD_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -21,6 +22,11 @@ struct rbffd_handle {
     cudaEvent_t ev[8] = {};
     cudaStream_t side = nullptr;  // overlaps the CSC export pattern with the weight solves
     cudaEvent_t side_ev[2] = {};
+    static constexpr int kClassStreams = 8;
+    cudaStream_t cls_st[kClassStreams] = {};  // one persistent solve launch per shape class
+    cudaEvent_t cls_ev[kClassStreams + 1] = {};
+    SolveTuner tuner;                         // per-class kernel and CTA size
+    std::string tune_report;
 };
 
 struct rbffd_opset {
@@ -112,6 +118,13 @@ __global__ void uniform_ptr(int64_t *a, int64_t n, int64_t step)
 // Shape classes of the mixed solve kernels: bin = 2 * (n > 32) + (m > 16) for n <= 64 and
 // m <= 32 (the register kernels' instantiations), NBIN - 1 for anything larger.
 constexpr int NBIN = 5;
+static_assert(NBIN <= rbffd_handle::kClassStreams, "one class stream per shape class");
+
+// Shape classes of one build run on forked streams (1) or one after another on the handle's
+// stream (0).
+#ifndef RBFFD_CLASS_CONCURRENT
+#define RBFFD_CLASS_CONCURRENT 1
+#endif
 __host__ __device__ inline int solve_bin(int n, int m)
 {
     if (n > 64 || m > 32) return NBIN - 1;
@@ -373,10 +386,12 @@ int ops_from_mask(uint32_t mask, int *ops)
     return n;
 }
 
-int autotune_wpb(rbffd_handle *h, size_t per_warp)
+// CTA size of the FP64 re-solve of the fallback queue (a small, irregular launch that the
+// autotuner does not time): the largest CTA (<= 8 warps) whose shared memory still lets >= 2
+// CTAs share an SM.
+int fallback_wpb(rbffd_handle *h, size_t per_warp)
 {
     if (h->opt.warps_per_block > 0) return h->opt.warps_per_block;
-    // Largest CTA (<= 8 warps) whose shared memory still lets >= 2 CTAs share an SM.
     const size_t budget = 110 * 1024;
     int w = 8;
     while (w > 1 && per_warp * w > budget) w >>= 1;
@@ -493,6 +508,8 @@ RBFFD_EXPORT int rbffd_create(const rbffd_options *opt, rbffd_handle **out)
         return RBFFD_ECUDA;
     }
     for (auto &ev : h->side_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (auto &cs : h->cls_st) cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (auto &ev : h->cls_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     *out = h;
     return RBFFD_OK;
 }
@@ -505,6 +522,8 @@ RBFFD_EXPORT void rbffd_destroy(rbffd_handle *h)
     cudaStreamSynchronize(h->side);
     for (auto &ev : h->ev) cudaEventDestroy(ev);
     for (auto &ev : h->side_ev) cudaEventDestroy(ev);
+    for (auto &ev : h->cls_ev) cudaEventDestroy(ev);
+    for (auto &cs : h->cls_st) cudaStreamDestroy(cs);
     cudaStreamDestroy(h->stream);
     cudaStreamDestroy(h->side);
     delete h;
@@ -514,6 +533,12 @@ RBFFD_EXPORT const char *rbffd_last_error(const rbffd_handle *h)
 {
     if (!h) return g_create_error.c_str();
     return h->err.c_str();
+}
+
+RBFFD_EXPORT const char *rbffd_autotune_report(const rbffd_handle *h)
+{
+    if (!h) return "";
+    return h->tune_report.c_str();
 }
 
 RBFFD_EXPORT void *rbffd_stream(rbffd_handle *h) { return h ? (void *)h->stream : nullptr; }
@@ -754,55 +779,65 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         a.fallback_list = fb_list;
         a.fallback_count = &dflags->fallback_count;
         a.hist = dflags->hist;
-        // one launch per shape class (per-node n / degree arrays), so that the many small
-        // stencils do not run with the shared-memory and register budget of the largest
-        std::vector<SolveArgs> launches;
-        if ((dn || ddeg) && nsys > 0) {
-            unsigned long long *cnt, hc[3 * NBIN];
-            int32_t *list;
-            CK(tmp.zeros(&cnt, 4 * NBIN));
-            CK(tmp.get(&list, nsys));
-            bin_count<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, cnt);
-            CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            BinOffsets bo;
-            int64_t o = 0;
-            for (int b = 0; b < NBIN; b++) {
-                bo.off[b] = o;
-                o += (int64_t)hc[b];
-            }
-            bin_scatter<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, bo,
-                                                    cnt + 3 * NBIN, list);
-            n_bin_launches = 2;
-            for (int b = 0; b < NBIN; b++) {
-                if (hc[b] == 0) continue;
-                SolveArgs ab = a;
-                ab.sys_list = list + bo.off[b];
-                ab.nsys = (int64_t)hc[b];
-                ab.max_n = (int)hc[NBIN + b];
-                ab.max_m = (int)hc[2 * NBIN + b];
-                ab.max_s = ab.max_n + ab.max_m;
-                launches.push_back(ab);
-            }
-        } else {
-            launches.push_back(a);
+    }
+    // Systems binned by shape class (per-node n / degree arrays), so that small stencils do
+    // not run with the shared-memory and register budget of the largest; each class is one
+    // persistent launch (warps claim systems from a counter) with the kernel and CTA size the
+    // autotuner chose for that class, and the classes' launches run on forked streams so that
+    // one class's tail overlaps the next class's start.
+    std::vector<SolveArgs> launches;
+    if ((dn || ddeg) && nsys > 0) {
+        unsigned long long *cnt, hc[3 * NBIN];
+        int32_t *list;
+        CK(tmp.zeros(&cnt, 4 * NBIN));
+        CK(tmp.get(&list, nsys));
+        bin_count<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, cnt);
+        CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        BinOffsets bo;
+        int64_t o = 0;
+        for (int b = 0; b < NBIN; b++) {
+            bo.off[b] = o;
+            o += (int64_t)hc[b];
         }
+        bin_scatter<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, bo,
+                                                cnt + 3 * NBIN, list);
+        n_bin_launches = 2;
+        for (int b = 0; b < NBIN; b++) {
+            if (hc[b] == 0) continue;
+            SolveArgs ab = a;
+            ab.sys_list = list + bo.off[b];
+            ab.nsys = (int64_t)hc[b];
+            ab.max_n = (int)hc[NBIN + b];
+            ab.max_m = (int)hc[2 * NBIN + b];
+            ab.max_s = ab.max_n + ab.max_m;
+            launches.push_back(ab);
+        }
+    } else {
+        launches.push_back(a);
+    }
+    {
         unsigned long long *claim;
         CK(tmp.zeros(&claim, launches.size()));
         for (size_t i = 0; i < launches.size(); i++) launches[i].next_sys = claim + i;
-        for (const SolveArgs &ab : launches) {
-            cudaError_t e = launch_solve_mixed_reg(ab, table, ab.max_m, 4, h->num_sms, st);
-            if (e == cudaErrorNotSupported) {
-                cudaGetLastError();
-                int wpb = autotune_wpb(h, solve_mixed_smem_per_warp(ab.max_s, ab.max_n, nops));
-                e = launch_solve_mixed(ab, table, wpb, h->num_sms, st);
+        std::vector<SolveConfig> cfg(launches.size());
+        for (size_t i = 0; i < launches.size(); i++)
+            CK(h->tuner.choose(launches[i], table, pb->precision, h->opt.warps_per_block, h->num_sms, st, &cfg[i]));
+        if (launches.size() == 1 || !RBFFD_CLASS_CONCURRENT) {
+            for (size_t i = 0; i < launches.size(); i++)
+                CK(launch_solve_config(launches[i], table, cfg[i], h->num_sms, st));
+        } else {
+            CK(cudaEventRecord(h->cls_ev[rbffd_handle::kClassStreams], st));
+            for (size_t i = 0; i < launches.size(); i++) {
+                cudaStream_t cs = h->cls_st[i];
+                CK(cudaStreamWaitEvent(cs, h->cls_ev[rbffd_handle::kClassStreams], 0));
+                CK(launch_solve_config(launches[i], table, cfg[i], h->num_sms, cs));
+                CK(cudaEventRecord(h->cls_ev[i], cs));
             }
-            CK(e);
+            for (size_t i = 0; i < launches.size(); i++) CK(cudaStreamWaitEvent(st, h->cls_ev[i], 0));
         }
         n_solve_launches = (int64_t)launches.size();
-    } else {
-        int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
-        CK(launch_solve_fp64(a, table, wpb, h->num_sms, st));
+        h->tune_report = h->tuner.report();
     }
     if (hook_on) {
         int rc2 = hook->download(h);
@@ -813,7 +848,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     CK(cudaMemcpyAsync(&hf, dflags, sizeof(Flags), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (pb->precision == RBFFD_PREC_MIXED && hf.fallback_count > 0 && !hf.knn_err) {
-        int wpb = autotune_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
+        int wpb = fallback_wpb(h, solve_fp64_smem_per_warp(max_s, max_n, nops));
         CK(launch_solve_fp64_subset(a, table, wpb, h->num_sms, st, hf.fallback_count));
         CK(cudaMemcpyAsync(&hf.first_bad, &dflags->first_bad, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     }

@@ -421,12 +421,111 @@ struct TopK {
         }
         refresh_kth();
     }
+
+    // Element p of the list (slot p / 32 of lane p % 32), read by every lane for its own p.
+    __device__ __forceinline__ void fetch(int p, unsigned long long &od, int &oi) const
+    {
+        const int src = p & 31, ss = p >> 5;
+        od = KEY_INF;
+        oi = INT_MAX;
+#pragma unroll
+        for (int s = 0; s < KS; s++) {
+            const unsigned long long v = __shfl_sync(RBFFD_FULL, d[s], src);
+            const int vi = __shfl_sync(RBFFD_FULL, id[s], src);
+            if (s == ss) {
+                od = v;
+                oi = vi;
+            }
+        }
+    }
+
+    // Merge 32 candidates sorted ascending across the lanes (lane j holds the j-th; unused
+    // lanes hold (KEY_INF, INT_MAX)) into the list, keeping its first 32 KS entries.  New
+    // element j goes to rank j + #{old < it}, old element p to p + #{new <= it}: a permutation
+    // (ties between equal padding keys aside, which are interchangeable).  The ranks are found
+    // by binary lifting with shuffles and the merged list is assembled in the warp's shared
+    // buffer (md, mi: 32 KS entries).
+    __device__ __forceinline__ void merge(unsigned long long cd, int ci, int lane, unsigned long long *md, int *mi)
+    {
+        constexpr int NL = 32 * KS;
+        int po = 0;
+#pragma unroll
+        for (int step = NL / 2; step >= 1; step >>= 1) {
+            unsigned long long od;
+            int oi;
+            fetch(po + step - 1, od, oi);
+            if (key_less(od, oi, cd, ci)) po += step;
+        }
+        {
+            unsigned long long od;
+            int oi;
+            fetch(po, od, oi);
+            if (key_less(od, oi, cd, ci)) po++;
+        }
+        const int rn = lane + po;
+        int ro[KS];
+#pragma unroll
+        for (int s = 0; s < KS; s++) {
+            int pn = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const unsigned long long nd = __shfl_sync(RBFFD_FULL, cd, pn + step - 1);
+                const int ni = __shfl_sync(RBFFD_FULL, ci, pn + step - 1);
+                if (!key_less(d[s], id[s], nd, ni)) pn += step;
+            }
+            const unsigned long long nd = __shfl_sync(RBFFD_FULL, cd, pn);
+            const int ni = __shfl_sync(RBFFD_FULL, ci, pn);
+            if (!key_less(d[s], id[s], nd, ni)) pn++;
+            ro[s] = s * 32 + lane + pn;
+        }
+        if (rn < NL) {
+            md[rn] = cd;
+            mi[rn] = ci;
+        }
+#pragma unroll
+        for (int s = 0; s < KS; s++)
+            if (ro[s] < NL) {
+                md[ro[s]] = d[s];
+                mi[ro[s]] = id[s];
+            }
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < KS; s++) {
+            d[s] = md[s * 32 + lane];
+            id[s] = mi[s * 32 + lane];
+        }
+        __syncwarp();
+        refresh_kth();
+    }
 };
+
+// Ascending bitonic sort of one (key, id) per lane across the warp.
+__device__ __forceinline__ void warp_sort32(unsigned long long &cd, int &ci, int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long od = __shfl_xor_sync(RBFFD_FULL, cd, j);
+            const int oi = __shfl_xor_sync(RBFFD_FULL, ci, j);
+            const bool want_min = ((lane & j) == 0) == ((lane & k) == 0);
+            const bool take = want_min ? key_less(od, oi, cd, ci) : key_less(cd, ci, od, oi);
+            if (take) {
+                cd = od;
+                ci = oi;
+            }
+        }
+    }
+}
+
+// Candidates of one batch that enter the list; at least this many are merged in bulk (sort +
+// merge, ~250 instructions) rather than inserted one at a time (~25 each).
+constexpr int MERGE_MIN = 10;
 
 // Exact FP64 keys of the queued candidates queue[0..cnt) (one per lane) and their insertion.
 template <int KS>
 __device__ __forceinline__ void take_queued(const GridDev &g, TopK<KS> &tk, const int64_t *queue, int cnt, double qx,
-                                            double qy, int lane)
+                                            double qy, int lane, unsigned long long *md, int *mi)
 {
     unsigned long long cd = KEY_INF;
     int ci = INT_MAX;
@@ -437,7 +536,17 @@ __device__ __forceinline__ void take_queued(const GridDev &g, TopK<KS> &tk, cons
         cd = (unsigned long long)__double_as_longlong(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
         ci = g.ids[t];
     }
-    unsigned m = __ballot_sync(RBFFD_FULL, key_less(cd, ci, tk.kd, tk.ki));
+    const bool enters = key_less(cd, ci, tk.kd, tk.ki);
+    unsigned m = __ballot_sync(RBFFD_FULL, enters);
+    if (__popc(m) >= MERGE_MIN) {
+        if (!enters) {
+            cd = KEY_INF;
+            ci = INT_MAX;
+        }
+        warp_sort32(cd, ci, lane);
+        tk.merge(cd, ci, lane, md, mi);
+        return;
+    }
     while (m) {
         const int src = __ffs(m) - 1;
         m &= m - 1;
@@ -454,7 +563,8 @@ __device__ __forceinline__ void take_queued(const GridDev &g, TopK<KS> &tk, cons
 // the survivors instead of all candidates.  The exact keys, and so the result, are unchanged.
 template <int KS>
 __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, int nseg, int64_t sa, int sl,
-                                               double qx, double qy, int cq, int64_t *queue, int lane)
+                                               double qx, double qy, int cq, int64_t *queue, int lane,
+                                               unsigned long long *md, int *mi)
 {
     // exclusive offsets of the segments
     int inc = sl;
@@ -501,7 +611,7 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
         qn += __popc(m);
         __syncwarp();
         if (qn >= 32) {
-            take_queued<KS>(g, tk, queue, 32, qx, qy, lane);
+            take_queued<KS>(g, tk, queue, 32, qx, qy, lane, md, mi);
             const int rest = qn - 32;
             const int64_t mv = lane < rest ? queue[32 + lane] : 0;
             __syncwarp();
@@ -510,12 +620,12 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
             __syncwarp();
         }
     }
-    if (qn > 0) take_queued<KS>(g, tk, queue, qn, qx, qy, lane);
+    if (qn > 0) take_queued<KS>(g, tk, queue, qn, qx, qy, lane, md, mi);
     __syncwarp();
 }
 
 template <int KS>
-__global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__restrict__ Q,
+__global__ void __launch_bounds__(256, (KS == 1 ? 4 : 2)) knn_kernel(GridDev g, const double2 *__restrict__ Q,
                                                   const int32_t *__restrict__ qcls,
                                                   const int32_t *__restrict__ q_node,
                                                   bool node_query, int64_t nq,
@@ -529,7 +639,11 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     __shared__ int64_t queue_all[8][64];  // survivors of the FP32 screen, per warp
+    __shared__ unsigned long long merge_d[8][32 * KS];  // bulk-merge buffers, per warp
+    __shared__ int merge_i[8][32 * KS];
     int64_t *queue = queue_all[threadIdx.x >> 5];
+    unsigned long long *md = merge_d[threadIdx.x >> 5];
+    int *mi = merge_i[threadIdx.x >> 5];
     for (int64_t q = warp; q < nq; q += nwarps) {
         // node queries: query q is node q_node[q] (or q) of the set; its coordinates, class,
         // stencil size and output row are taken by node id.  Point queries: Q[q], class 0.
@@ -565,12 +679,17 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
                         sa = g.start[c0];
                         sl = g.start[c1] - g.start[c0];
                     }
-                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane);
+                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane, md, mi);
                 }
             } else {
-                // ring: bottom row, top row (full width), then left/right cells of the middle rows
+                // ring: bottom row, top row (full width), then left/right cells of the middle rows.
+                // A segment whose FP32 lower bound of the distance to q is beyond the current
+                // k-th distance (an FP32 upper bound of it) is skipped: none of its nodes can
+                // enter.  The bound carries the same margins as the stopping test below.
                 int nmid = 2 * R - 1;
                 int nseg_all = 2 + 2 * nmid;
+                const float kd32 = f64_to_f32(__longlong_as_double((long long)tk.kd)) * (1.0f + 0x1p-20f);
+                const float mg = 0x1p-20f * (float)(R + 1) * cs32;
                 for (int s0 = 0; s0 < nseg_all; s0 += 32) {
                     int nseg = min(32, nseg_all - s0);
                     int64_t sa = 0;
@@ -587,13 +706,28 @@ __global__ void __launch_bounds__(256) knn_kernel(GridDev g, const double2 *__re
                             row = cy - R + 1 + r;
                             xa = xb = ((s - 2) & 1) ? cx + R : cx - R;
                         }
-                        if (row >= 0 && row < g.ny && xa <= xb && xa >= 0 && xb < g.nx) {
+                        bool far = false;
+                        if (kd32 < CUDART_INF_F) {
+                            float gx = 0.0f, gy;
+                            if (s < 2) {
+                                gy = s == 0 ? fmaf((float)(R - 1), cs32, fy) : fmaf((float)R, cs32, -fy);
+                            } else {
+                                gx = ((s - 2) & 1) ? fmaf((float)R, cs32, -fx) : fmaf((float)(R - 1), cs32, fx);
+                                const int dyc = row - cy;
+                                gy = dyc < 0 ? fmaf((float)(-dyc - 1), cs32, fy)
+                                             : (dyc > 0 ? fmaf((float)dyc, cs32, -fy) : 0.0f);
+                            }
+                            gx = fmaxf(gx - mg, 0.0f);
+                            gy = fmaxf(gy - mg, 0.0f);
+                            far = fmaf(gx, gx, gy * gy) * (1.0f - 0x1p-18f) > kd32;
+                        }
+                        if (!far && row >= 0 && row < g.ny && xa <= xb && xa >= 0 && xb < g.nx) {
                             int c0 = row * g.nx + xa, c1 = row * g.nx + xb + 1;
                             sa = g.start[c0];
                             sl = g.start[c1] - g.start[c0];
                         }
                     }
-                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane);
+                    sweep_segments<KS>(g, tk, nseg, sa, sl, qp.x, qp.y, cq, queue, lane, md, mi);
                 }
             }
             // distance from q to the unsearched cells: to the sides of the searched square

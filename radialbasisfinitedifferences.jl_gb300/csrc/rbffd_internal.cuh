@@ -173,8 +173,8 @@ struct SolveArgs {
     int max_refine;
     double refine_tol;
     int unscaled_overload;     // generate_operator(X,p,n,polydeg) quirk
-    unsigned long long *next_sys;  // nullable, zeroed: the mixed Schur kernel claims systems from
-                                   // this counter instead of a fixed grid stride
+    unsigned long long *next_sys;  // nullable, zeroed: the solve kernels claim systems from this
+                                   // counter instead of a fixed grid stride
 };
 
 cudaError_t launch_solve_fp64(const SolveArgs &a, const OpTable &ops, int warps_per_block,

@@ -597,14 +597,39 @@ __device__ __forceinline__ void df_mac(float a, float d, float &s_hi, float &s_l
     s_lo += err + e;
 }
 
+// The packed Phi and P of a system rewritten in place as their double-float splits (float2
+// (hi, lo) in the same 8 bytes per element), for the later residuals of a system with a single
+// evaluation row: its FP64 first residual, the only user of the exact FP64 values, is done.
+__device__ __forceinline__ void presplit_phi_p(double *phiP, double *P, int n, int m, int lane)
+{
+    const int nphi = tri_off(n);
+    for (int e = lane; e < nphi; e += 32) reinterpret_cast<float2 *>(phiP)[e] = df_from_f64(phiP[e]);
+    for (int e = lane; e < n * m; e += 32) reinterpret_cast<float2 *>(P)[e] = df_from_f64(P[e]);
+    __syncwarp();
+}
+
+// Element `ad` of an FP64 array as (hi, lo): split on the fly, or read when PRE (the array was
+// rewritten by presplit_phi_p).
+template <bool PRE>
+__device__ __forceinline__ void split_at(const double *a, int ad, float &hi, float &lo)
+{
+    if constexpr (PRE) {
+        const float2 v = reinterpret_cast<const float2 *>(a)[ad];
+        hi = v.x;
+        lo = v.y;
+    } else {
+        split_f64(a[ad], hi, lo);
+    }
+}
+
 // Residual after a correction, r_new = r_old - A d, without FP64 instructions: d (the last
 // correction, R32) is a float vector, A = hi + lo splits exactly enough, A d is accumulated as
 // a double-float sum and subtracted from r_old, itself a double-float pair.  The error of
 // A d is ~2^-44 |A||d| with |d| ~ 1e-5 |x|, and the pair holds r_old to 2^-47 of its size
 // (~1e-5 |A||x|), both far below FP64 rounding of |A||x|, so the refinement converges as with
 // an FP64 residual.  B holds r_old as (hi, lo) pairs and receives r_new; R32 receives hi.  Phi rows lane-per-row (the split of Phi_ij shared by the row's
-// operators), P' rows lane-per-element.
-template <int SP, int SM, int RMAX>
+// operators), P' rows lane-per-element.  PRE: Phi and P hold their splits already.
+template <int SP, int SM, int RMAX, bool PRE>
 __device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, double *B,
                                             float *R32, int lane)
 {
@@ -623,7 +648,7 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
             const int ad = jj <= ii ? offi + jj : offj + ii;
             offj += jj + 1;
             float ah, al;
-            split_f64(phiP[ad], ah, al);
+            split_at<PRE>(phiP, ad, ah, al);
             const float *dj = R32 + jj * r;
 #pragma unroll
             for (int q = 0; q < RMAX; q++) {
@@ -636,7 +661,7 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
         }
         for (int l = 0; l < m; l++) {
             float ah, al;
-            split_f64(P[ii * m + l], ah, al);
+            split_at<PRE>(P, ii * m + l, ah, al);
             const float *dl = R32 + (n + l) * r;
 #pragma unroll
             for (int q = 0; q < RMAX; q++) {
@@ -658,7 +683,7 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
             const int l = e / r, q = e - l * r;
             for (int jj = 0; jj < n; jj++) {
                 float ah, al;
-                split_f64(P[jj * m + l], ah, al);
+                split_at<PRE>(P, jj * m + l, ah, al);
                 const float d = R32[jj * r + q];
                 df_mac(ah, d, th[u], tl[u]);
                 tl[u] = fmaf(al, d, tl[u]);
@@ -965,6 +990,10 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
         if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, xf, lane);
         int64_t r0, r1;
         system_rows(a, sys, j, r0, r1);
+        // a system with one evaluation row (the collocated case) needs its exact FP64 Phi and P
+        // only for that row's first residual; the later residuals then read them pre-split
+        const bool one_row = r1 - r0 == 1;
+        bool presplit = false;
         int iters_max = 0;
         for (int64_t t = r0; t < r1 && !fallback; t++) {
             const int64_t row = row_id(a, t);
@@ -980,8 +1009,14 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) 
                     __syncwarp();
                 } else if (it == 1) {
                     residual_schur(phiP, P, n, m, r, B, X, R32, true, lane);
+                } else if (one_row) {
+                    if (!presplit) {
+                        presplit_phi_p(phiP, P, n, m, lane);
+                        presplit = true;
+                    }
+                    residual_df<SP, SM, RMAX, true>(phiP, P, n, m, r, B, R32, lane);
                 } else {
-                    residual_df<SP, SM, RMAX>(phiP, P, n, m, r, B, R32, lane);
+                    residual_df<SP, SM, RMAX, false>(phiP, P, n, m, r, B, R32, lane);
                 }
                 schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
                 // x0 is kept as FP64 for the FP64 first residual; from the first update on, x is

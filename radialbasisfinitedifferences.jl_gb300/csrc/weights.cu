@@ -48,8 +48,17 @@ __global__ void __launch_bounds__(256) solve_fp64_kernel(SolveArgs a, OpTable op
     int64_t nwork = subset ? (int64_t)*subset_count : a.nsys;
     int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t w = gw; w < nwork; w += nw) {
-        int64_t sys = subset ? (int64_t)subset[w] : w;
+    // systems claimed from a counter when one is given (persistent CTAs even out the tail),
+    // else a fixed grid stride
+    const bool claim = a.next_sys && !subset;
+    auto next = [&](int64_t cur) -> int64_t {
+        if (!claim) return cur + nw;
+        unsigned long long v = 0ull;
+        if (lane == 0) v = atomicAdd(a.next_sys, 1ull);
+        return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
+    };
+    for (int64_t w = claim ? next(0) : gw; w < nwork; w = next(w)) {
+        int64_t sys = subset ? (int64_t)subset[w] : (a.sys_list ? (int64_t)a.sys_list[w] : w);
         int j = a.sys_node[sys];
         int n = a.n_node ? a.n_node[j] : a.n;
         int deg = a.deg_node ? a.deg_node[j] : a.deg;
@@ -110,7 +119,13 @@ __global__ void __launch_bounds__(256) solve_mixed_kernel(SolveArgs a, OpTable o
 
     int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t ts = gw; ts < a.nsys; ts += nw) {
+    auto next = [&](int64_t cur) -> int64_t {
+        if (!a.next_sys) return cur + nw;
+        unsigned long long v = 0ull;
+        if (lane == 0) v = atomicAdd(a.next_sys, 1ull);
+        return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
+    };
+    for (int64_t ts = a.next_sys ? next(0) : gw; ts < a.nsys; ts = next(ts)) {
         const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
         int j = a.sys_node[sys];
         int n = a.n_node ? a.n_node[j] : a.n;

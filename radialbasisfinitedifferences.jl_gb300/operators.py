@@ -37,6 +37,11 @@ class Handle:
     def synchronize(self):
         nat.check(self.ptr, self._lib.rbffd_synchronize(self.ptr))
 
+    def autotune_report(self):
+        """The solve autotuner's per-class choices on this handle (rbffd_autotune_report)."""
+        r = self._lib.rbffd_autotune_report(self.ptr)
+        return [ln for ln in (r.decode() if r else "").splitlines() if ln]
+
     def close(self):
         if self.ptr:
             self._lib.rbffd_destroy(self.ptr)
