@@ -47,7 +47,9 @@ def parse():
                          "classes (2,097,152 nodes); rk4: advection-diffusion-hyperviscosity RK4 on 2048^2 nodes")
     ap.add_argument("--total", type=int, default=2_097_152, help="uneven: number of nodes")
     ap.add_argument("--rk-nx", type=int, default=2048, help="rk4: grid side")
-    ap.add_argument("--rk-steps", type=int, default=100, help="rk4: time steps per precision")
+    ap.add_argument("--rk-steps", type=int, default=1000, help="rk4: time steps per precision")
+    ap.add_argument("--no-uneven", action="store_true", help="headline line without the uneven-batch block")
+    ap.add_argument("--no-rk4", action="store_true", help="headline line without the time-stepping block")
     ap.add_argument("--rk-fields", type=int, default=64, help="rk4: fields advanced together")
     return ap.parse_args()
 
@@ -66,6 +68,15 @@ def workload_name(nx):
 # CSR output, so it scales with the systems) and the SELL SpMV on 1024x1024 nodes (31.46 M nnz).
 NCU_TRAFFIC = {"solve_bytes_per_system": (46.59e6 + 174.67e6) / 262144,
                "spmv_bytes_per_nnz": (385.90e6 + 4.11e6) / 31457280}
+
+
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth of MEASURED_PEAKS.json, else the fallback."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm = json.load(open(path)).get("hbm_gbs") if os.path.exists(path) else None
+    if hbm:
+        return float(hbm), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback 6800 GB/s"
 
 
 def dist_env():
@@ -177,6 +188,32 @@ def cpu_sample_rate(X, target_s, nthreads=0, seed=0):
         size = min(len(X), int(size * max(2.0, target_s / max(dt, 1e-3))))
 
 
+def cpu_description():
+    """CPU model, logical core count and the oracle's compiler flags (oracle/Makefile)."""
+    model = None
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+            for line in out.splitlines():
+                if line.startswith("Model name:"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    flags = None
+    for line in open(os.path.join(ROOT, "oracle", "Makefile")):
+        if line.startswith("CFLAGS"):
+            flags = line.split("=", 1)[1].strip()
+    return {"cpu_model": model, "host_cores": os.cpu_count(), "compiler": "gcc", "compiler_flags": flags}
+
+
 def cpu_phases(X, solve_rate, seed=11):
     """Per-phase CPU times of the oracle at the full node count: kNN of every node (all
     threads), the weight solves (extrapolated from the sampled rate), sparse(I, J, V) of one
@@ -230,6 +267,7 @@ def run_reference(args):
             times.append(time.perf_counter() - t0)
     ms = 1e3 * float(np.mean(times))
     value = size / (ms * 1e-3)
+    rate1, size1, dt1 = cpu_sample_rate(X, max(2.0, args.cpu_seconds / 2), nthreads=1, seed=1)
     phases = cpu_phases(X, value) if not args.no_cpu_phases else None
     sample = (f"{size} random rows of the {len(X)}-node workload per step (stencils, explicit "
               f"inverse of the 40x40 system, weights of Dx/Dy/Lap), C oracle port, {cores} threads")
@@ -250,7 +288,8 @@ def run_reference(args):
         "config": {"workload": workload_name(args.nx), "rows_per_step": size,
                    "parallelism": f"host cores x{cores}"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
-                         "phases_ms_full_size": phases},
+                         "value_1_thread": rate1, "sample_1_thread": f"{size1} random rows, 1 thread, {dt1:.1f} s",
+                         "phases_ms_full_size": phases, **cpu_description()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -461,9 +500,14 @@ def run_ours(args):
         from oracle import oracle as orc
 
         rate, size, dt = cpu_sample_rate(X_host[: rows_per] if ws == 1 else X_host, args.cpu_seconds)
+        rate1, size1, dt1 = cpu_sample_rate(X_host[: rows_per] if ws == 1 else X_host, args.cpu_seconds / 2,
+                                            nthreads=1, seed=1)
         cpu = {"value": rate, "unit": "solves/s", "cores": orc.max_threads(), "kind": "port",
                "sample": f"{size} random rows of the {rows_per}-node workload (kNN, explicit inverse, Dx/Dy/Lap "
-                         f"weights), C oracle port, {dt:.1f} s"}
+                         f"weights), C oracle port, {dt:.1f} s",
+               "value_1_thread": rate1,
+               "sample_1_thread": f"{size1} random rows, 1 thread, {dt1:.1f} s",
+               **cpu_description()}
 
     manu = manufactured_errors(pkg, h)
     m = 10
@@ -476,10 +520,7 @@ def run_ours(args):
     nres = sum(i * c for i, c in enumerate(hist)) / max(1, sum(hist))
     fp64_flops_sys = n * m + n * 3 * 12 + 2 * (s_ * s_ - m * m) * 3 + (nres + 1) * s_ * 3
     solve_ach = rows_per * fp64_flops_sys / (solve_ms * 1e-3) / 1e12
-    hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs") if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
-    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800 GB/s"
-    hbm = hbm or 6800.0
+    hbm, hbm_src = hbm_peak()
     out = {
         "metric": METRIC,
         "value": value,
@@ -518,6 +559,7 @@ def run_ours(args):
         "phases_ms": {"knn": knn_ms, "solve_mixed": solve_ms, "spmv_per_op": spmv_ms,
                       "grid": float(np.mean([s["ms_grid"] for s in st_mixed]))},
         "measured_fma_peaks_tflops": {"fp64": fp64_peak.value, "fp32": fp32_peak.value},
+        "solve_autotune": h.autotune_report(),
         "roofline": {
             "kernel": "solve_mixed_schur_kernel",
             "bound": "fp64",
@@ -545,12 +587,17 @@ def run_ours(args):
         },
         "cpu_baseline": cpu,
     }
+    # the uneven-batch and time-stepping workloads, measured after the headline (one GPU)
+    if ws == 1 and not args.no_uneven:
+        out["uneven"] = uneven_block(uneven_results(args, 2, 1))
+    if ws == 1 and not args.no_rk4:
+        out["rk4"] = rk4_block(rk4_results(args))
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
 
 
-def run_uneven(args):
+def uneven_results(args, steps, warmup):
     """Mixed stencil sizes, boundary and ghost classes: rectangle [0,2]x[0,1] with 4 boundaries
     and one ghost layer, per-node (k, deg) in {(20,2), (30,3), (45,4), (60,5)} (85% (30,3)),
     boundary-class-masked kNN, Dx/Dy/Lap with PHS r^3 and Dxk/Dyk (K=4) with PHS r^5; mixed
@@ -573,16 +620,16 @@ def run_uneven(args):
     for name, (p, ops, kd) in sets.items():
         for prec in ("mixed", "fp64"):
             ts, st = [], None
-            for it in range(args.warmup + args.steps):
+            for it in range(warmup + steps):
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 s = pkg.OperatorSet(Xd, None, p, 0, 0, ops=ops, precision=prec, node_class=cd, n_per_node=nd,
                                     deg_per_node=ddev, k_deriv=kd, handle=h, device=True)
                 torch.cuda.synchronize()
-                if it >= args.warmup:
+                if it >= warmup:
                     ts.append(time.perf_counter() - t0)
                 st = s.stats.as_dict()
-                if it == args.warmup + args.steps - 1:
+                if it == warmup + steps - 1:
                     rp = s.device_csr(ops[0])[0]
                     rpt = torch.as_tensor(pkg.operators._DeviceArray(rp, s.rows + 1, "<i8"), device="cuda").clone()
                     vals[(name, prec)] = ([s.device_values(o).clone() for o in ops], rpt)
@@ -608,12 +655,37 @@ def run_uneven(args):
     out = {"workload": "uneven: rectangle [0,2]x[0,1], 4 boundaries + ghosts, per-node (k,deg) "
                        "{(20,2),(30,3),(45,4),(60,5)}, boundary-masked kNN",
            "nodes": int(len(X)), "counts": d["counts"],
-           "steps": args.steps, "warmup": args.warmup, "timing": "wall clock of the whole device build, "
-           "inputs resident in HBM", **res}
-    print(json.dumps(out))
+           "steps": steps, "warmup": warmup, "timing": "wall clock of the whole device build, "
+           "inputs resident in HBM", "solve_autotune": h.autotune_report(), **res}
+    h.close()
+    return out
 
 
-def run_rk4(args):
+def uneven_block(u):
+    """The uneven workload's figures for the headline line."""
+    blk = {"workload": u["workload"], "nodes": u["nodes"], "per_class": u["counts"]["per_class"],
+           "boundary_nodes": u["counts"]["boundary"], "ghost_nodes": u["counts"]["ghost"]}
+    for name, label in (("ops", "Dx,Dy,Lap (r^3)"), ("hyperviscosity", "Dxk,Dyk (r^5, K=4)")):
+        mx, f64 = u[f"{name}_mixed"], u[f"{name}_fp64"]
+        blk[name] = {
+            "operators": label,
+            "solves_per_s_mixed": mx["solves_per_s"], "solves_per_s_fp64": f64["solves_per_s"],
+            "ms_build_mixed": mx["ms_per_build"], "ms_build_fp64": f64["ms_per_build"],
+            "ms_solve_mixed": mx["ms_solve"] + mx["ms_fallback"], "ms_solve_fp64": f64["ms_solve"],
+            "mixed_over_fp64_solves": f64["ms_solve"] / (mx["ms_solve"] + mx["ms_fallback"]),
+            "mixed_over_fp64_build": f64["ms_per_build"] / mx["ms_per_build"],
+            "row_rel_err_mixed_vs_fp64": u[f"{name}_row_rel_err_mixed_vs_fp64"],
+            "fallback_fraction": mx["fallback"] / u["nodes"], "refine_hist": mx["refine_hist"],
+        }
+    blk["solve_autotune"] = u["solve_autotune"]
+    return blk
+
+
+def run_uneven(args):
+    print(json.dumps(uneven_results(args, args.steps, args.warmup)))
+
+
+def rk4_results(args):
     """du/dt = L u, L = -a.grad + nu Lap - gamma (Dxk + Dyk), a = (1, 0.5), nu = 1e-3,
     gamma = 100 h^4 (examples/adv_diff_test.jl:152), Dxk/Dyk with K = 4 and PHS r^5; RK4 with
     dt = 0.2 h (reduced to the largest stable step when rho(L) dt exceeds RK4's real-axis
@@ -675,33 +747,55 @@ def run_rk4(args):
     out.update({"rho_L": lam, "dt_nominal": dt, "rho_dt_nominal": lam * dt, "rk4_limit": limit,
                 "stable_at_nominal_dt": bool(stable), "dt_used": dt_used})
     res = {}
+    stream = torch.cuda.ExternalStream(h.stream)
+    hbm = hbm_peak()[0]
     for dt_name, tdt in (("f64", torch.float64), ("f32", torch.float32)):
-        u = u0.to(tdt).contiguous()
+        u = u0.to(tdt).contiguous().clone()
         rk[dt_name].run(u, dt_used, 2)  # warm-up (graph capture)
-        u = u0.to(tdt).contiguous()
+        u = u0.to(tdt).contiguous().clone()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t_w = time.perf_counter()
-        e0.record()
+        e0.record(stream)
         rk[dt_name].run(u, dt_used, args.rk_steps)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = (time.perf_counter() - t_w) * 1e3
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
         res[dt_name] = (u, ms)
         sz = 8 if dt_name == "f64" else 4
         nnz = s3.nnz
+        # the stencil application of one stage: weights and column ids once, the fields read
+        # once and the stage result written once
         stage_bytes = nnz * (sz + 4) + 2 * N * F * sz
+        gbps = 4 * args.rk_steps * stage_bytes / (ms * 1e-3) / 1e9
         out[f"{dt_name}"] = {"ms_per_step": ms / args.rk_steps, "steps": args.rk_steps,
-                             "stage_algorithmic_GBps": 4 * args.rk_steps * stage_bytes / (ms * 1e-3) / 1e9,
+                             "stage_algorithmic_bytes": stage_bytes,
+                             "stage_algorithmic_GBps": gbps, "stage_frac_of_hbm": gbps / hbm,
                              "stage_fma_TFLOPs": 4 * args.rk_steps * 2.0 * nnz * F / (ms * 1e-3) / 1e12,
                              "finite": bool(torch.isfinite(u).all().item())}
     u64, u32 = res["f64"][0], res["f32"][0].double()
     out["drift_f32_vs_f64"] = float(((u32 - u64).norm() / u64.norm()).item())
+    out["hbm_peak_GBps"] = hbm
     for r in rk.values():
         r.close()
     s3.close()
     s5.close()
-    print(json.dumps(out))
+    h.close()
+    return out
+
+
+def rk4_block(r):
+    """The time-stepping workload's figures for the headline line."""
+    keys = ("workload", "nodes", "fields", "nnz_per_operator", "fixed_rows", "rho_L", "dt_nominal",
+            "rho_dt_nominal", "stable_at_nominal_dt", "dt_used", "drift_f32_vs_f64", "hbm_peak_GBps")
+    blk = {k: r[k] for k in keys}
+    for p in ("f64", "f32"):
+        blk[p] = {k: r[p][k] for k in ("ms_per_step", "steps", "stage_algorithmic_GBps", "stage_frac_of_hbm",
+                                       "stage_fma_TFLOPs", "finite")}
+    return blk
+
+
+def run_rk4(args):
+    print(json.dumps(rk4_results(args)))
 
 
 def main():

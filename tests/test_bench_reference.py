@@ -27,6 +27,8 @@ def test_reference_arm_json_line():
     assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["value_1_thread"] > 0 and cb["host_cores"] >= 1
+    assert cb["cpu_model"] and "-O3" in cb["compiler_flags"] and "-march=native" not in cb["compiler_flags"]
     ph = cb["phases_ms_full_size"]
     for k in ("knn_all_nodes", "solves_all_nodes_extrapolated", "csc_build_per_op", "spmv_csc_1_thread",
               "spmv_rows_all_threads"):
