@@ -221,11 +221,19 @@ int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, 
    sparsity pattern; e.g. {Dx, Dy, Lap} with r^3 and {HV} with r^5).  fixed_rows (host,
    nullable, rows bytes): rows held at their initial values (du = 0), the Dirichlet
    overwrite of examples/adv_diff_test.jl:166-167.  dtype 0: FP64 weights and fields,
-   1: FP32.  Fields are row-major [rows][nfields] device arrays. */
+   1: FP32.  Fields are row-major [rows][nfields] device arrays.  FP32 with nfields in
+   {4, 8, 16, 32, 64, 128} applies L tile by tile from shared memory (tiles of 64 rows of a
+   Z-curve order of the nodes, each tile's stencil-column union staged by asynchronous
+   copies) and in difference form, sum_t w_t (v_t - v_i) + (sum_t w_t) v_i, whose FP32 error
+   scales with the field's differences rather than its size. */
 int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int nsets, const double *coef,
                      const uint8_t *fixed_rows, int nfields, int dtype, rbffd_rk4 **out);
 /* Advance u (device, in place) by nsteps steps of size dt.  Pairs of steps run as one
-   captured CUDA graph (4 fused stage kernels per step), re-captured when u or dt change. */
+   captured CUDA graph (4 fused stage kernels per step), re-captured when u or dt change.
+   Without ghost closures L is constant and a classic RK4 step equals the degree-4 Taylor
+   polynomial of exp(dt L); it is evaluated in Horner form (u + dt/4 L u, then u + dt/3 L w,
+   u + dt/2 L w, u + dt L w), which needs no stage accumulator.  With closures the stage form
+   is used. */
 int rbffd_rk4_run(rbffd_handle *h, rbffd_rk4 *rk, void *u, double dt, int64_t nsteps);
 /* y = L x for the stepper's fields (x, y device [rows][nfields]). */
 int rbffd_rk4_apply(rbffd_handle *h, rbffd_rk4 *rk, const void *x, void *y);

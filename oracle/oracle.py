@@ -21,6 +21,7 @@ OPS = {"E": 0, "Dx": 1, "Dy": 2, "Dxx": 3, "Dyy": 4, "Dxy": 5, "Lap": 6, "Dxk": 
 ORC_ESINGULAR = 3
 
 _lib = None
+_all_threads = None  # OpenMP threads of the host, read before any call narrows them
 
 
 def build(force=False):
@@ -51,8 +52,17 @@ def lib():
         L.orc_phi.argtypes = [i32, i32, i32, ctypes.c_double, ctypes.c_double]
         L.orc_phi.restype = ctypes.c_double
         L.orc_max_threads.restype = i32
+        global _all_threads
+        _all_threads = L.orc_max_threads()
         _lib = L
     return _lib
+
+
+def _threads(nthreads):
+    """The thread count a call runs with: nthreads, or all host threads when 0 (the C side
+    keeps the last count it was given, so 0 is passed on as an explicit count)."""
+    lib()
+    return int(nthreads) if nthreads else _all_threads
 
 
 def _p(a):
@@ -79,7 +89,9 @@ class OracleError(RuntimeError):
 
 
 def max_threads():
-    return lib().orc_max_threads()
+    """OpenMP threads of the host (all of them, whatever a previous call narrowed them to)."""
+    lib()
+    return _all_threads
 
 
 def knn(X, Q, k, cls_x=None, cls_q=None, nthreads=0, brute=False):
@@ -91,7 +103,7 @@ def knn(X, Q, k, cls_x=None, cls_q=None, nthreads=0, brute=False):
     if brute:
         rc = lib().orc_knn_brute(_p(X), len(X), _p(Q), len(Q), k, _p(cls_x), _p(cls_q), _p(idx), _p(d2))
     else:
-        rc = lib().orc_knn(_p(X), len(X), _p(Q), len(Q), k, _p(cls_x), _p(cls_q), _p(idx), _p(d2), nthreads)
+        rc = lib().orc_knn(_p(X), len(X), _p(Q), len(Q), k, _p(cls_x), _p(cls_q), _p(idx), _p(d2), _threads(nthreads))
     if rc:
         raise OracleError(rc, "knn")
     return idx, d2
@@ -112,7 +124,7 @@ def generate(X, Y, p, n, deg, ops, cls=None, k_deriv=0, use_inverse=True, nthrea
     bad = ctypes.c_int64(-1)
     rc = lib().orc_generate(
         _p(X), N, _p(Y), M, p, n, deg, _p(_cls(cls)), len(opv), _p(opv), k_deriv, int(use_inverse),
-        _p(nbr), _p(nn), _p(cols), _p(W), ctypes.byref(bad), nthreads,
+        _p(nbr), _p(nn), _p(cols), _p(W), ctypes.byref(bad), _threads(nthreads),
     )
     if rc:
         raise OracleError(rc, "generate", bad.value)
@@ -130,7 +142,7 @@ def generate_unscaled(X, p, n, deg, ops, k_deriv=0, use_inverse=True, nthreads=0
     bad = ctypes.c_int64(-1)
     rc = lib().orc_generate_unscaled(
         _p(X), N, p, n, deg, len(opv), _p(opv), k_deriv, int(use_inverse), _p(cols), _p(W),
-        ctypes.byref(bad), nthreads,
+        ctypes.byref(bad), _threads(nthreads),
     )
     if rc:
         raise OracleError(rc, "generate_unscaled", bad.value)
@@ -156,7 +168,7 @@ def spmv_rows(cols, W, x, nthreads=0):
     W = np.ascontiguousarray(W, dtype=np.float64)
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.empty(cols.shape[0], np.float64)
-    lib().orc_spmv_rows(cols.shape[0], cols.shape[1], _p(cols), _p(W), _p(x), _p(y), nthreads)
+    lib().orc_spmv_rows(cols.shape[0], cols.shape[1], _p(cols), _p(W), _p(x), _p(y), _threads(nthreads))
     return y
 
 

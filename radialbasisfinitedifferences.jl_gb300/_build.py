@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "librbffd.so")
 SOURCES = ["api.cu", "knn.cu", "weights.cu", "weights_reg.cu", "weights_reg64.cu", "weights_reg64_m16_r4.cu",
            "weights_reg64_m16_r8.cu", "weights_reg64_m32_r4.cu", "weights_reg64_m32_r8.cu", "sparse.cu", "peaks.cu",
-           "knn_noalloc.cu", "tune.cu"]
+           "knn_noalloc.cu", "tune.cu", "rk4_tiled.cu", "weights_reg48_r4.cu", "weights_reg48_r8.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3",

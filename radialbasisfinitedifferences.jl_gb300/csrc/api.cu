@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "rbffd_internal.cuh"
+#include "rk4_tiled.cuh"
 #include "tune.cuh"
 
 #define RBFFD_EXPORT extern "C" __attribute__((visibility("default")))
@@ -1099,6 +1100,8 @@ struct rbffd_rk4 {
     int32_t *order = nullptr;  // rows in Morton (Z-curve) order of their nodes
     std::vector<rbffd_ghost *> closures;  // applied to every stage input, in order
     void *unext = nullptr, *wA = nullptr, *wB = nullptr, *acc = nullptr;
+    TileOp tiles;  // FP32 tiled stage layout (rk4_tiled.cu), when `tiled`
+    bool tiled = false;
     cudaGraphExec_t graph2 = nullptr;  // two steps u -> unext -> u
     const void *graph_u = nullptr;
     double graph_dt = 0.0;
@@ -1117,10 +1120,43 @@ cudaError_t rk4_closures(rbffd_rk4 *rk, void *w, cudaStream_t st)
     return cudaSuccess;
 }
 
-// Enqueue one RK4 step u -> out on stream st; the ghost closures are applied to every stage
-// input first (u itself for the first stage, as the reference's cons_sys overwrites u).
+// One Horner stage out = u + c L v (held rows: out = u), on the tiled FP32 kernel when the
+// stepper has the tile layout and the buffers are 16-byte aligned.
+cudaError_t rk4_horner_stage(rbffd_handle *h, rbffd_rk4 *rk, const void *v, const void *u, void *out, double c,
+                             cudaStream_t st)
+{
+    const bool aligned = ((((uintptr_t)v) | ((uintptr_t)u) | ((uintptr_t)out)) & 15u) == 0;
+    if (rk->tiled && aligned)
+        return launch_tile_stage(rk->tiles, (const float *)v, (const float *)u, (float *)out, rk->F, c, h->num_sms,
+                                 st);
+    const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
+    return launch_rk4_stage(rk->rows, rk->order, rk->row_ptr, rk->col, val, v, u, rk->acc, out, rk->fixed, rk->F, c,
+                            3, rk->dtype, h->num_sms, st);
+}
+
+// Enqueue one RK4 step u -> out on stream st.
+//
+// Without ghost closures the system du/dt = L u (rows held fixed have zero rows in L) is linear
+// with a constant operator, and classic RK4's step is then exactly the degree-4 Taylor
+// polynomial of exp(dt L):  u + dt L u + dt^2/2 L^2 u + dt^3/6 L^3 u + dt^4/24 L^4 u.  It is
+// evaluated in Horner form,
+//     w1 = u + dt/4 L u,  w2 = u + dt/3 L w1,  w3 = u + dt/2 L w2,  out = u + dt L w3,
+// four operator applications as in the stage form, without the stage-sum accumulator (each
+// stage reads v and u and writes one array).  With closures, the closures are applied to every
+// stage input first (u itself for the first stage, as the reference's cons_sys overwrites u),
+// which is not a constant linear map between stages, so the classic stage form is used.
 cudaError_t rk4_enqueue_step(rbffd_handle *h, rbffd_rk4 *rk, void *u, void *out, double dt, cudaStream_t st)
 {
+    if (rk->closures.empty()) {
+        const void *in[4] = {u, rk->wA, rk->wB, rk->wA};
+        void *o[4] = {rk->wA, rk->wB, rk->wA, out};
+        const double c[4] = {0.25 * dt, dt / 3.0, 0.5 * dt, dt};
+        for (int i = 0; i < 4; i++) {
+            cudaError_t e = rk4_horner_stage(h, rk, in[i], u, o[i], c[i], st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
     const void *val = rk->dtype == 0 ? (const void *)rk->val64 : (const void *)rk->val32;
     struct Stage {
         void *w, *o;
@@ -1233,6 +1269,61 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
     if (fixed_rows) {
         CKB(keep.get(&rk->fixed, rk->rows));
         CKB(cudaMemcpyAsync(rk->fixed, fixed_rows, rk->rows, cudaMemcpyHostToDevice, st));
+    }
+    if (dtype == 1 && tile_stage_supported(nfields)) {
+        // FP32 tile layout: tiles of 64 consecutive rows of the Z-curve order, each tile's
+        // stencil-column union, 16-bit slots (rk4_tiled.cu)
+        int kmax = s0->uniform ? s0->n : 0;
+        if (!s0->uniform) {
+            std::vector<int64_t> hp(rk->rows + 1);
+            CKB(cudaMemcpyAsync(hp.data(), rk->row_ptr, sizeof(int64_t) * (rk->rows + 1), cudaMemcpyDeviceToHost, st));
+            CKB(cudaStreamSynchronize(st));
+            for (int64_t i = 0; i < rk->rows; i++) kmax = std::max<int>(kmax, (int)(hp[i + 1] - hp[i]));
+        }
+        TileOp t;
+        t.T = 64;
+        t.KP = (kmax + 3) & ~3;  // whole quads of entries
+        t.ntile = (rk->rows + t.T - 1) / t.T;
+        int32_t *cnt;
+        int *bad;
+        CKB(tmp.get(&cnt, t.ntile));
+        CKB(tmp.zeros(&bad, 1));
+        CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 0, cnt,
+                              bad, h->num_sms, st));
+        std::vector<int32_t> hc(t.ntile);
+        int hbad = 0;
+        CKB(cudaMemcpyAsync(hc.data(), cnt, sizeof(int32_t) * t.ntile, cudaMemcpyDeviceToHost, st));
+        CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CKB(cudaStreamSynchronize(st));
+        std::vector<int32_t> hu(t.ntile + 1);
+        int64_t tot = 0;
+        for (int64_t i = 0; i < t.ntile; i++) {
+            hu[i] = (int32_t)tot;
+            tot += hc[i];
+            t.ucap = std::max(t.ucap, hc[i]);
+        }
+        hu[t.ntile] = (int32_t)tot;
+        int smem_max = 0;
+        cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+        if (!hbad && tot < INT32_MAX && tile_stage_smem(t, nfields) <= (size_t)smem_max) {
+            int32_t *uptr;
+            CKB(keep.get(&uptr, t.ntile + 1));
+            CKB(keep.get(&t.uni, tot));
+            CKB(keep.get(&t.w, (size_t)t.ntile * t.T * t.KP));
+            CKB(keep.get(&t.slot, (size_t)t.ntile * t.T * t.KP));
+            CKB(keep.get(&t.rowinfo, (size_t)t.ntile * t.T));
+            CKB(cudaMemcpyAsync(uptr, hu.data(), sizeof(int32_t) * (t.ntile + 1), cudaMemcpyHostToDevice, st));
+            t.uptr = uptr;
+            CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 1,
+                                  cnt, bad, h->num_sms, st));
+            CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CKB(cudaStreamSynchronize(st));
+            if (!hbad && tile_stage_prepare(t, nfields) == cudaSuccess) {
+                rk->tiles = t;
+                rk->tiled = true;
+            }
+            cudaGetLastError();
+        }
     }
     size_t fb = (size_t)rk->rows * nfields * (dtype == 0 ? 8 : 4);
     char *bufs;

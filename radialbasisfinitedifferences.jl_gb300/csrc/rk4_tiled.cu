@@ -1,0 +1,482 @@
+// Tiled FP32 stencil application for the RK4 stages of du/dt = L u on F fields (the
+// right-hand side of examples/adv_diff_test.jl:151-152 applied to many fields at once).
+//
+// The per-row stage kernels of sparse.cu gather, for every row, its k neighbours' field rows
+// (F values each) through L1/L2: 30 gathers of a 256-byte row per output row at F = 64, which
+// makes them L1-throughput bound at ~20 % of HBM.  Here rows are grouped into tiles of T
+// consecutive rows of the Z-curve order (spatially compact blocks of nodes).  The union of a
+// tile's stencil columns (~2.6 T columns for T = 64, k = 30) is copied into shared memory once
+// per stage by asynchronous 16-byte copies (cp.async.cg, L2 only) spread over all threads of
+// the CTA, double-buffered so that the next tile's copies run while the current tile is
+// computed.  (One TMA bulk copy per 256-byte field row was measured first: 172 small bulk
+// copies per tile held a tile to ~7 us, about three times its compute time.)  Column ids are
+// stored per tile as 16-bit slots into that union, so an entry costs 4 + 2 bytes of HBM
+// instead of 4 + 4.
+//
+// The sum is evaluated in difference form against a reference node of the tile,
+//     (L v)_i = sum_t w_t (v_{c_t} - v_ref) + s_i v_ref,   s_i = sum_t w_t (FP64 row sum),
+// which equals the plain sum in exact arithmetic.  The operator's rows nearly sum to zero (it
+// is made of derivatives) while its weights are large (nu/h^2, gamma/h^4), so the plain FP32
+// sum loses digits to cancellation; the differences of a smooth field across a tile are
+// small, and their FP32 products carry an error proportional to them instead of to |v|.
+//
+// Stage (Horner form of classic RK4 for a constant operator, see api.cu):
+//     out_i = u_i + c (L v)_i  on free rows,   out_i = u_i on held rows.
+#include "rbffd_internal.cuh"
+#include "rk4_tiled.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Tile build: sort each tile's stencil column ids, keep the distinct ones (the union), map
+// every entry to its slot in the union.  One CTA per tile; P (a power of two >= T * KP) keys
+// in shared memory.
+// ---------------------------------------------------------------------------------------
+__device__ void block_bitonic_sort(int32_t *key, int P)
+{
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const int32_t a = key[i], b = key[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        key[i] = b;
+                        key[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Exclusive block scan of one int per thread; returns the prefix, *total gets the sum.
+__device__ int block_scan_excl(int v, int *sh, int *total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(RBFFD_FULL, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) sh[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int s = lane < nw ? sh[lane] : 0;
+        int si = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(RBFFD_FULL, si, o);
+            if (lane >= o) si += t;
+        }
+        if (lane < nw) sh[lane] = si - s;
+        if (lane == nw - 1) sh[32] = si;
+    }
+    __syncthreads();
+    const int r = inc - v + sh[w];
+    *total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t v)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// mode 0: cnt[tile] = union size.  mode 1: union ids, entry slots and weights, self slots and
+// row sums.  bad: set when a row's own node is not in its stencil (the difference form needs
+// it) or a union exceeds 65535 slots.
+__global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows, const int32_t *__restrict__ order,
+                                                         const int64_t *__restrict__ row_ptr,
+                                                         const int32_t *__restrict__ col,
+                                                         const float *__restrict__ val32,
+                                                         const double *__restrict__ val64,
+                                                         const uint8_t *__restrict__ fixed, int P, int mode,
+                                                         int32_t *__restrict__ cnt, int *bad)
+{
+    extern __shared__ __align__(16) int32_t tb_smem[];
+    int32_t *key = tb_smem;     // P
+    int32_t *uq = tb_smem + P;  // P (mode 1)
+    __shared__ int sh[33];
+    __shared__ uint16_t selfs[256];  // T <= 256
+    const int T = t.T, KP = t.KP;
+    for (int64_t tile = blockIdx.x; tile < t.ntile; tile += gridDim.x) {
+        for (int e = threadIdx.x; e < P; e += blockDim.x) {
+            int32_t id = INT_MAX;
+            if (e < T * KP) {
+                const int i = e / KP, k = e - i * KP;
+                const int64_t gi = tile * T + i;
+                if (gi < rows) {
+                    const int32_t r = order[gi];
+                    const int64_t a = row_ptr[r];
+                    if (k < (int)(row_ptr[r + 1] - a)) id = col[a + k];
+                }
+            }
+            key[e] = id;
+        }
+        __syncthreads();
+        block_bitonic_sort(key, P);
+        // distinct keys: a contiguous chunk of P / blockDim per thread
+        const int per = P / blockDim.x, b0 = threadIdx.x * per;
+        int c = 0;
+        for (int e = b0; e < b0 + per; e++) c += key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1]);
+        int total;
+        int pos = block_scan_excl(c, sh, &total);
+        if (mode == 0) {
+            if (threadIdx.x == 0) {
+                cnt[tile] = total;
+                if (total > 65535) atomicOr(bad, 2);
+            }
+            __syncthreads();
+            continue;
+        }
+        const int32_t ubase = t.uptr[tile];
+        for (int e = b0; e < b0 + per; e++) {
+            if (key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1])) {
+                uq[pos] = key[e];
+                t.uni[ubase + pos] = key[e];
+                pos++;
+            }
+        }
+        __syncthreads();
+        // row record: the row, its FP64 row sum (as FP32), its own slot, whether it is held
+        for (int i = threadIdx.x; i < T; i += blockDim.x) {
+            const int64_t gi = tile * T + i;
+            int4 ri = make_int4(-1, 0, 0, 0);
+            uint16_t self = 0;
+            if (gi < rows) {
+                const int32_t r = order[gi];
+                const int s = lower_bound_i32(uq, total, r);
+                if (s >= total || uq[s] != r) atomicOr(bad, 1);
+                self = (uint16_t)(s < total ? s : 0);
+                double acc = 0.0;
+                for (int64_t a = row_ptr[r]; a < row_ptr[r + 1]; a++) acc += val64[a];
+                ri = make_int4(r, __float_as_int((float)acc), self, (fixed && fixed[r]) ? 1 : 0);
+            }
+            selfs[i] = self;
+            t.rowinfo[gi] = ri;
+        }
+        __syncthreads();
+        // entries: slot into the union and FP32 weight; padding entries point at the row's own
+        // slot with weight 0 (their difference is exactly 0)
+        for (int e = threadIdx.x; e < T * KP; e += blockDim.x) {
+            const int i = e / KP, k = e - i * KP;
+            const int64_t gi = tile * T + i;
+            uint16_t slot = 0;
+            float wv = 0.0f;
+            if (gi < rows) {
+                const int32_t r = order[gi];
+                const int64_t a = row_ptr[r];
+                slot = selfs[i];
+                if (k < (int)(row_ptr[r + 1] - a)) {
+                    slot = (uint16_t)lower_bound_i32(uq, total, col[a + k]);
+                    wv = val32[a + k];
+                }
+            }
+            t.slot[tile * (int64_t)T * KP + e] = slot;
+            t.w[tile * (int64_t)T * KP + e] = wv;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Stage kernel.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// 16-byte asynchronous global -> shared copy through L2 (LDGSTS), completion tracked per thread
+// by commit groups.
+__device__ __forceinline__ void cp16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+struct StageArgs {
+    TileOp t;
+    const float *v;      // stage input, gathered (rows x F)
+    const float *u;      // RK4 state (rows x F); may equal v
+    float *out;          // rows x F
+    float c;
+    // shared-memory layout of one buffer: union field rows, weights, slots, row records, the
+    // tile's own rows of u, the reference row, column ids (the union's, then the tile's rows)
+    uint32_t wofs, sofs, rofs, uofs, refofs, idofs, bufbytes;
+};
+
+// The copies of one tile into `buf`, spread over all threads in 16-byte pieces: the union's
+// field rows of v, the tile's own rows of u, the tile's reference row of v (its middle row, or
+// its first when the tile is short), the weights, the slots and the row records, from the ids
+// in `ids` (a shared-memory list filled one tile ahead: U union columns, then the T rows); one
+// commit group per thread and tile.  After these land the tile is computed from shared memory.
+template <int LPR>
+__device__ __forceinline__ void issue_tile(const StageArgs &s, int64_t tile, int U, const int32_t *ids,
+                                           unsigned char *buf)
+{
+    constexpr int F = 4 * LPR;
+    const TileOp &t = s.t;
+    for (int c = threadIdx.x; c < U * LPR; c += blockDim.x) {
+        const int row = c / LPR, part = c % LPR;
+        cp16(buf + (size_t)c * 16, s.v + (size_t)ids[row] * F + 4 * part);
+    }
+    for (int c = threadIdx.x; c < t.T * LPR; c += blockDim.x) {
+        const int row = c / LPR, part = c % LPR;
+        const int32_t r = ids[U + row];
+        if (r >= 0) cp16(buf + s.uofs + (size_t)c * 16, s.u + (size_t)r * F + 4 * part);
+    }
+    if ((int)threadIdx.x < LPR) {
+        int32_t r = ids[U + t.T / 2];
+        if (r < 0) r = ids[U];
+        cp16(buf + s.refofs + (size_t)threadIdx.x * 16, s.v + (size_t)r * F + 4 * threadIdx.x);
+    }
+    const int eb = t.T * t.KP;
+    const unsigned char *wsrc = reinterpret_cast<const unsigned char *>(t.w + (size_t)tile * eb);
+    for (int c = threadIdx.x; c < eb / 4; c += blockDim.x) cp16(buf + s.wofs + (size_t)c * 16, wsrc + (size_t)c * 16);
+    const unsigned char *ssrc = reinterpret_cast<const unsigned char *>(t.slot + (size_t)tile * eb);
+    for (int c = threadIdx.x; c < eb / 8; c += blockDim.x) cp16(buf + s.sofs + (size_t)c * 16, ssrc + (size_t)c * 16);
+    const int4 *rsrc = t.rowinfo + (size_t)tile * t.T;
+    for (int c = threadIdx.x; c < t.T; c += blockDim.x) cp16(buf + s.rofs + (size_t)c * 16, rsrc + c);
+    cp_commit();
+}
+
+// The ids list of a tile: its union's columns, then its rows (-1 past the end of the order).
+// Loads up to two union ids and one row per thread into registers (issued early, stored late).
+struct TileIds {
+    int32_t a = 0, U = 0, id0 = 0, id1 = 0, row = -1;
+    __device__ void load(const TileOp &t, int64_t tile)
+    {
+        a = t.uptr[tile];
+        U = t.uptr[tile + 1] - a;
+        if ((int)threadIdx.x < U) id0 = t.uni[a + threadIdx.x];
+        if ((int)threadIdx.x + (int)blockDim.x < U) id1 = t.uni[a + threadIdx.x + blockDim.x];
+        if ((int)threadIdx.x < t.T) row = t.rowinfo[tile * t.T + threadIdx.x].x;
+    }
+    __device__ void store(const TileOp &t, int32_t *ids) const
+    {
+        if ((int)threadIdx.x < U) ids[threadIdx.x] = id0;
+        if ((int)threadIdx.x + (int)blockDim.x < U) ids[threadIdx.x + blockDim.x] = id1;
+        for (int i = threadIdx.x + 2 * blockDim.x; i < U; i += blockDim.x) ids[i] = t.uni[a + i];
+        if ((int)threadIdx.x < t.T) ids[U + threadIdx.x] = row;
+    }
+};
+
+__device__ __forceinline__ float4 f4_fma(float a, float4 x, float4 y)
+{
+    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+__device__ __forceinline__ float4 f4_sub(float4 a, float4 b)
+{
+    return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ float4 f4_add(float4 a, float4 b)
+{
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// One stage over all tiles.  LPR = F / 4 lanes per row (one float4 of fields each), 32 / LPR rows
+// per warp and pass.  Persistent CTAs walk the tiles with a stride of gridDim.x.  Software
+// pipeline per tile k: issue the copies of tile k + 1 (into the other buffer, with the ids
+// stored one tile earlier), load the ids of tile k + 2 into registers, wait for this thread's
+// copies of tile k, barrier, subtract the reference row from the union rows, barrier, compute
+// tile k from shared memory, store the ids of tile k + 2, barrier.
+//
+// Difference form against a tile-wide reference row v_ref (a node of the tile):
+//     (L v)_i = sum_t w_t (v_{c_t} - v_ref) + s_i v_ref,   s_i = sum_t w_t (FP64 row sum),
+// equal to the plain sum in exact arithmetic; the differences of a smooth field across a tile
+// are small, so the FP32 products carry an error proportional to them instead of to |v|, and
+// the subtraction is paid once per union row and tile instead of once per entry.
+template <int LPR>
+__global__ void __launch_bounds__(512, 1) rk4_tile_stage_kernel(StageArgs s)
+{
+    extern __shared__ __align__(128) unsigned char ts_smem[];
+    constexpr int RPW = 32 / LPR;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int sub = lane / LPR, sl = lane - sub * LPR;
+    const TileOp &t = s.t;
+    const int T = t.T, KQ = t.KP >> 2;
+    const int64_t G = gridDim.x;
+    int64_t tile = blockIdx.x;
+    if (tile >= t.ntile) return;
+    auto bufp = [&](int b) { return ts_smem + (size_t)b * s.bufbytes; };
+    auto idsp = [&](int b) { return reinterpret_cast<int32_t *>(bufp(b) + s.idofs); };
+    int U0 = 0, U1 = 0;  // union sizes of the tiles whose ids sit in buffers 0 and 1
+    {
+        TileIds cur;
+        cur.load(t, tile);
+        cur.store(t, idsp(0));
+        U0 = cur.U;
+        if (tile + G < t.ntile) {
+            TileIds nx;
+            nx.load(t, tile + G);
+            nx.store(t, idsp(1));
+            U1 = nx.U;
+        }
+    }
+    __syncthreads();
+    issue_tile<LPR>(s, tile, U0, idsp(0), bufp(0));
+    for (int k = 0; tile < t.ntile; k++, tile += G) {
+        const int b = k & 1;
+        unsigned char *buf = bufp(b);
+        const int U = b ? U1 : U0;
+        const int64_t nxt = tile + G, n2 = nxt + G;
+        if (nxt < t.ntile) issue_tile<LPR>(s, nxt, b ? U0 : U1, idsp(b ^ 1), bufp(b ^ 1));
+        TileIds pre;
+        if (n2 < t.ntile) pre.load(t, n2);
+        if (nxt < t.ntile)
+            cp_wait<1>();
+        else
+            cp_wait<0>();
+        __syncthreads();
+        float4 *fb = reinterpret_cast<float4 *>(buf);
+        const float4 *ref = reinterpret_cast<const float4 *>(buf + s.refofs);
+        {
+            const float4 rv = ref[threadIdx.x % LPR];  // blockDim is a multiple of LPR
+            for (int c = threadIdx.x; c < U * LPR; c += blockDim.x) fb[c] = f4_sub(fb[c], rv);
+        }
+        __syncthreads();
+        const float4 vref = ref[sl];
+        const float4 *ub = reinterpret_cast<const float4 *>(buf + s.uofs);
+        const float4 *wbase = reinterpret_cast<const float4 *>(buf + s.wofs);
+        const uint2 *sbase = reinterpret_cast<const uint2 *>(buf + s.sofs);
+        const int4 *rinfo = reinterpret_cast<const int4 *>(buf + s.rofs);
+        for (int rl0 = 0; rl0 < T; rl0 += nw * RPW) {
+            const int rl = rl0 + warp * RPW + sub;
+            if (rl >= T) continue;
+            const int4 ri = rinfo[rl];
+            if (ri.x < 0) continue;
+            const float4 uo = ub[rl * LPR + sl];
+            float4 o = uo;
+            if (!ri.w) {
+                const float rs = __int_as_float(ri.y);
+                float4 acc0 = make_float4(rs * vref.x, rs * vref.y, rs * vref.z, rs * vref.w);
+                float4 acc1 = make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 *wr = wbase + rl * KQ;
+                const uint2 *sr = sbase + rl * KQ;
+#pragma unroll 2
+                for (int q = 0; q < KQ; q++) {
+                    const float4 wv = wr[q];
+                    const uint2 sv = sr[q];
+                    const float4 x0 = fb[(int)(sv.x & 0xffffu) * LPR + sl];
+                    const float4 x1 = fb[(int)(sv.x >> 16) * LPR + sl];
+                    const float4 x2 = fb[(int)(sv.y & 0xffffu) * LPR + sl];
+                    const float4 x3 = fb[(int)(sv.y >> 16) * LPR + sl];
+                    acc0 = f4_fma(wv.x, x0, acc0);
+                    acc1 = f4_fma(wv.y, x1, acc1);
+                    acc0 = f4_fma(wv.z, x2, acc0);
+                    acc1 = f4_fma(wv.w, x3, acc1);
+                }
+                o = f4_fma(s.c, f4_add(acc0, acc1), uo);
+            }
+            reinterpret_cast<float4 *>(s.out)[(int64_t)ri.x * LPR + sl] = o;
+        }
+        if (n2 < t.ntile) {
+            pre.store(t, idsp(b));
+            if (b)
+                U1 = pre.U;
+            else
+                U0 = pre.U;
+        }
+        __syncthreads();
+    }
+}
+
+// Shared memory of one buffer (offsets in StageArgs).
+void stage_layout(const TileOp &t, int F, StageArgs &s)
+{
+    auto up128 = [](uint32_t b) { return (b + 127u) & ~127u; };
+    s.wofs = up128((uint32_t)t.ucap * (uint32_t)F * 4u);
+    s.sofs = s.wofs + up128((uint32_t)t.T * t.KP * 4u);
+    s.rofs = s.sofs + up128((uint32_t)t.T * t.KP * 2u);
+    s.uofs = s.rofs + up128((uint32_t)t.T * 16u);
+    s.refofs = s.uofs + up128((uint32_t)t.T * (uint32_t)F * 4u);
+    s.idofs = s.refofs + up128((uint32_t)F * 4u);
+    s.bufbytes = up128(s.idofs + (uint32_t)(t.ucap + t.T) * 4u);
+}
+
+int build_keys(const TileOp &t)
+{
+    int P = 256;
+    while (P < t.T * t.KP) P <<= 1;
+    return P;
+}
+
+}  // namespace
+
+cudaError_t launch_tile_build(TileOp &t, int64_t rows, const int32_t *order, const int64_t *row_ptr,
+                              const int32_t *col, const float *val32, const double *val64, const uint8_t *fixed,
+                              int mode, int32_t *cnt, int *bad, int num_sms, cudaStream_t st)
+{
+    if (t.T > 256) return cudaErrorInvalidValue;
+    const int P = build_keys(t);
+    const size_t smem = (size_t)2 * P * sizeof(int32_t);
+    cudaError_t e = cudaFuncSetAttribute(tile_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int64_t blocks = t.ntile < (int64_t)num_sms * 8 ? t.ntile : (int64_t)num_sms * 8;
+    if (blocks < 1) blocks = 1;
+    tile_build_kernel<<<(int)blocks, 256, smem, st>>>(t, rows, order, row_ptr, col, val32, val64, fixed, P, mode, cnt,
+                                                     bad);
+    return cudaGetLastError();
+}
+
+size_t tile_stage_smem(const TileOp &t, int F)
+{
+    StageArgs s{};
+    stage_layout(t, F, s);
+    return (size_t)2 * s.bufbytes;
+}
+
+bool tile_stage_supported(int F) { return F == 4 || F == 8 || F == 16 || F == 32 || F == 64 || F == 128; }
+
+cudaError_t tile_stage_prepare(const TileOp &t, int F)
+{
+    const int smem = (int)tile_stage_smem(t, F);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    switch (F) {
+    case 4: return cudaFuncSetAttribute(rk4_tile_stage_kernel<1>, a, smem);
+    case 8: return cudaFuncSetAttribute(rk4_tile_stage_kernel<2>, a, smem);
+    case 16: return cudaFuncSetAttribute(rk4_tile_stage_kernel<4>, a, smem);
+    case 32: return cudaFuncSetAttribute(rk4_tile_stage_kernel<8>, a, smem);
+    case 64: return cudaFuncSetAttribute(rk4_tile_stage_kernel<16>, a, smem);
+    case 128: return cudaFuncSetAttribute(rk4_tile_stage_kernel<32>, a, smem);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_tile_stage(const TileOp &t, const float *v, const float *u, float *out, int F, double c,
+                              int num_sms, cudaStream_t st)
+{
+    if (t.ntile <= 0) return cudaSuccess;
+    StageArgs s{};
+    s.t = t;
+    s.v = v;
+    s.u = u;
+    s.out = out;
+    s.c = (float)c;
+    stage_layout(t, F, s);
+    const size_t smem = (size_t)2 * s.bufbytes;
+    const int blocks = (int)(t.ntile < (int64_t)num_sms ? t.ntile : (int64_t)num_sms);
+    switch (F) {
+    case 4: rk4_tile_stage_kernel<1><<<blocks, 512, smem, st>>>(s); break;
+    case 8: rk4_tile_stage_kernel<2><<<blocks, 512, smem, st>>>(s); break;
+    case 16: rk4_tile_stage_kernel<4><<<blocks, 512, smem, st>>>(s); break;
+    case 32: rk4_tile_stage_kernel<8><<<blocks, 512, smem, st>>>(s); break;
+    case 64: rk4_tile_stage_kernel<16><<<blocks, 512, smem, st>>>(s); break;
+    case 128: rk4_tile_stage_kernel<32><<<blocks, 512, smem, st>>>(s); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}

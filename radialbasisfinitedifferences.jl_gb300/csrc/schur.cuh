@@ -38,9 +38,13 @@ namespace {
 constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never updated
 
 // Resident CTAs of 4 warps per SM requested for stencils of <= 32 nodes (4: <= 128 registers
-// per thread, 16 warps per SM).
+// per thread, 16 warps per SM) and of 33..48 nodes (2: the 2 x 48 register-resident Phi^-1
+// entries fit without spills).
 #ifndef RBFFD_SCHUR_MIN_BLOCKS
 #define RBFFD_SCHUR_MIN_BLOCKS 4
+#endif
+#ifndef RBFFD_SCHUR48_MIN_BLOCKS
+#define RBFFD_SCHUR48_MIN_BLOCKS 2
 #endif
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
@@ -633,7 +637,7 @@ template <int SP, int SM, int RMAX, bool PRE>
 __device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, double *B,
                                             float *R32, int lane)
 {
-    constexpr int NS = SP / 32;
+    constexpr int NS = RegRows<SP>::NS;
     float sh[NS][RMAX], sl[NS][RMAX];
 #pragma unroll
     for (int k = 0; k < NS; k++) {
@@ -916,7 +920,8 @@ __device__ __forceinline__ void write_row_df(const SolveArgs &a, const OpTable &
 }
 
 template <int SP, int SM, int RMAX>
-__global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : 2)) solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
+__global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : (SP <= 48 ? RBFFD_SCHUR48_MIN_BLOCKS : 2)))
+    solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1109,6 +1114,9 @@ cudaError_t launch_schur_sp32(const SolveArgs &a, const OpTable &ops, int SM, in
                               cudaStream_t st);
 cudaError_t launch_schur_sp64(const SolveArgs &a, const OpTable &ops, int SM, int RMAX, int wpb, int num_sms,
                               cudaStream_t st);
+// Stencils of 33..48 nodes with at most 16 monomials (weights_reg48_r<RMAX>.cu).
+cudaError_t launch_schur_48_16_4(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);
+cudaError_t launch_schur_48_16_8(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);
 size_t schur_smem_per_warp(int SP, int SM, int max_n, int max_m, int nops);
 // The four 64-node instantiations, one per translation unit (weights_reg64_m<SM>_r<RMAX>.cu).
 cudaError_t launch_schur_64_16_4(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st);

@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t rows, const int64_t *
 //   mode 0 (stage 1): acc  = v;          wnext = u + c v
 //   mode 1 (stage 2, 3): acc += 2 v;     wnext = u + c v
 //   mode 2 (stage 4): unext = u + c (acc + v)        (c = dt / 6)
+//   mode 3 (any stage of the Horner form, see api.cu): out = u + c v  (no accumulator)
 // Rows are visited in `order` (a spatial locality order of the nodes): a CTA takes chunks of
 // 64 consecutive rows of that order and its 8 warps work on neighbouring rows together, so the
 // gathered rows of w (F values each) are shared through L1 instead of being re-read from L2.
@@ -220,8 +221,10 @@ __global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int3
                     } else if (mode == 1) {
                         acc[o + f] = fma((T)2, v0, acc[o + f]);
                         out[o + f] = fma(c, v0, u[o + f]);
-                    } else {
+                    } else if (mode == 2) {
                         out[o + f] = fma(c, acc[o + f] + v0, u[o + f]);
+                    } else {
+                        out[o + f] = fma(c, v0, u[o + f]);
                     }
                 }
                 if (g < F) {
@@ -231,8 +234,10 @@ __global__ void __launch_bounds__(256) rk4_stage_kernel(int64_t rows, const int3
                     } else if (mode == 1) {
                         acc[o + g] = fma((T)2, v1, acc[o + g]);
                         out[o + g] = fma(c, v1, u[o + g]);
-                    } else {
+                    } else if (mode == 2) {
                         out[o + g] = fma(c, acc[o + g] + v1, u[o + g]);
+                    } else {
+                        out[o + g] = fma(c, v1, u[o + g]);
                     }
                 }
             }
@@ -359,8 +364,10 @@ __global__ void __launch_bounds__(256) rk4_stage_vec_kernel(int64_t rows, const 
             } else if (mode == 1) {
                 *pa = VT::fma1((T)2, v, *pa);
                 *po = VT::fma1(c, v, uu);
-            } else {
+            } else if (mode == 2) {
                 *po = VT::fma1(c, VT::add(*pa, v), uu);
+            } else {
+                *po = VT::fma1(c, v, uu);
             }
         }
     }

@@ -1,6 +1,7 @@
 // Mixed-precision weight solves with the Schur-complement FP32 preconditioner (schur.cuh):
 // instantiations for stencils of at most 32 nodes and the dispatcher used by the operator
-// builder.  Stencils of 33..64 nodes are instantiated in weights_reg64.cu.
+// builder.  Stencils of 33..48 nodes (at most 16 monomials) are instantiated in
+// weights_reg48_r<RMAX>.cu, the rest up to 64 nodes in weights_reg64*.cu.
 #include "schur.cuh"
 
 size_t schur_smem_per_warp(int SP, int SM, int max_n, int max_m, int nops)
@@ -36,5 +37,7 @@ cudaError_t launch_solve_mixed_reg(const SolveArgs &a, const OpTable &ops, int m
     const int SM = a.max_m <= 16 ? 16 : 32;
     const int RMAX = r <= 4 ? 4 : 8;
     if (a.max_n <= 32) return launch_schur_sp32(a, ops, SM, RMAX, wpb, num_sms, st);
+    if (a.max_n <= 48 && SM == 16)
+        return RMAX == 4 ? launch_schur_48_16_4(a, ops, wpb, num_sms, st) : launch_schur_48_16_8(a, ops, wpb, num_sms, st);
     return launch_schur_sp64(a, ops, SM, RMAX, wpb, num_sms, st);
 }
