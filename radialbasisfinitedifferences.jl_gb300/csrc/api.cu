@@ -1282,40 +1282,45 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
         }
         TileOp t;
         t.T = 64;
-        t.KP = (kmax + 3) & ~3;  // whole quads of entries
+        t.KP = kmax;
         t.ntile = (rk->rows + t.T - 1) / t.T;
-        int32_t *cnt;
+        int32_t *cnt, *cnt2;
         int *bad;
         CKB(tmp.get(&cnt, t.ntile));
+        CKB(tmp.get(&cnt2, t.ntile));
         CKB(tmp.zeros(&bad, 1));
         CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 0, cnt,
-                              bad, h->num_sms, st));
-        std::vector<int32_t> hc(t.ntile);
+                              cnt2, bad, h->num_sms, st));
+        std::vector<int32_t> hc(t.ntile), hc2(t.ntile);
         int hbad = 0;
         CKB(cudaMemcpyAsync(hc.data(), cnt, sizeof(int32_t) * t.ntile, cudaMemcpyDeviceToHost, st));
+        CKB(cudaMemcpyAsync(hc2.data(), cnt2, sizeof(int32_t) * t.ntile, cudaMemcpyDeviceToHost, st));
         CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
         CKB(cudaStreamSynchronize(st));
         std::vector<int32_t> hu(t.ntile + 1);
         int64_t tot = 0;
+        int kpp = 0;
         for (int64_t i = 0; i < t.ntile; i++) {
             hu[i] = (int32_t)tot;
             tot += hc[i];
             t.ucap = std::max(t.ucap, hc[i]);
+            kpp = std::max(kpp, hc2[i]);
         }
         hu[t.ntile] = (int32_t)tot;
+        t.KPP = (kpp + 3) & ~3;  // whole quads of merged entries
         int smem_max = 0;
         cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
         if (!hbad && tot < INT32_MAX && tile_stage_smem(t, nfields) <= (size_t)smem_max) {
             int32_t *uptr;
             CKB(keep.get(&uptr, t.ntile + 1));
             CKB(keep.get(&t.uni, tot));
-            CKB(keep.get(&t.w, (size_t)t.ntile * t.T * t.KP));
-            CKB(keep.get(&t.slot, (size_t)t.ntile * t.T * t.KP));
+            CKB(keep.get(&t.pw, (size_t)t.ntile * (t.T / 2) * t.KPP));
+            CKB(keep.get(&t.pslot, (size_t)t.ntile * (t.T / 2) * t.KPP));
             CKB(keep.get(&t.rowinfo, (size_t)t.ntile * t.T));
             CKB(cudaMemcpyAsync(uptr, hu.data(), sizeof(int32_t) * (t.ntile + 1), cudaMemcpyHostToDevice, st));
             t.uptr = uptr;
             CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 1,
-                                  cnt, bad, h->num_sms, st));
+                                  cnt, cnt2, bad, h->num_sms, st));
             CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
             CKB(cudaStreamSynchronize(st));
             if (!hbad && tile_stage_prepare(t, nfields) == cudaSuccess) {

@@ -95,23 +95,29 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t 
     return lo;
 }
 
-// mode 0: cnt[tile] = union size.  mode 1: union ids, entry slots and weights, self slots and
-// row sums.  bad: set when a row's own node is not in its stencil (the difference form needs
-// it) or a union exceeds 65535 slots.
+// mode 0: cnt[tile] = union size, cnt2[tile] = the largest merged entry count of its row
+// pairs.  mode 1: union ids, row records and the merged pair entries.  Rows 2j and 2j + 1 of a
+// tile form pair j: their stencils are merged into one list of (slot, w_2j, w_2j+1) with a
+// zero weight where a row does not use the column, so that the stage reads each neighbour row
+// once for both rows.  bad |= 2 when a union exceeds 65535 slots.
 __global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows, const int32_t *__restrict__ order,
                                                          const int64_t *__restrict__ row_ptr,
                                                          const int32_t *__restrict__ col,
                                                          const float *__restrict__ val32,
                                                          const double *__restrict__ val64,
                                                          const uint8_t *__restrict__ fixed, int P, int mode,
-                                                         int32_t *__restrict__ cnt, int *bad)
+                                                         int32_t *__restrict__ cnt, int32_t *__restrict__ cnt2,
+                                                         int *bad)
 {
     extern __shared__ __align__(16) int32_t tb_smem[];
-    int32_t *key = tb_smem;     // P
-    int32_t *uq = tb_smem + P;  // P (mode 1)
-    __shared__ int sh[33];
-    __shared__ uint16_t selfs[256];  // T <= 256
     const int T = t.T, KP = t.KP;
+    int32_t *key = tb_smem;                                          // P
+    int32_t *uq = key + P;                                           // P
+    float *rw = reinterpret_cast<float *>(uq + P);                   // T x KP row weights
+    uint16_t *rslot = reinterpret_cast<uint16_t *>(rw + T * KP);     // T x KP row slots
+    __shared__ int sh[33];
+    __shared__ int rlen[256];  // T <= 256
+    __shared__ int maxm;
     for (int64_t tile = blockIdx.x; tile < t.ntile; tile += gridDim.x) {
         for (int e = threadIdx.x; e < P; e += blockDim.x) {
             int32_t id = INT_MAX;
@@ -126,6 +132,7 @@ __global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows,
             }
             key[e] = id;
         }
+        if (threadIdx.x == 0) maxm = 0;
         __syncthreads();
         block_bitonic_sort(key, P);
         // distinct keys: a contiguous chunk of P / blockDim per thread
@@ -134,59 +141,90 @@ __global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows,
         for (int e = b0; e < b0 + per; e++) c += key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1]);
         int total;
         int pos = block_scan_excl(c, sh, &total);
-        if (mode == 0) {
-            if (threadIdx.x == 0) {
-                cnt[tile] = total;
-                if (total > 65535) atomicOr(bad, 2);
-            }
-            __syncthreads();
-            continue;
-        }
-        const int32_t ubase = t.uptr[tile];
+        const int32_t ubase = mode ? t.uptr[tile] : 0;
         for (int e = b0; e < b0 + per; e++) {
             if (key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1])) {
                 uq[pos] = key[e];
-                t.uni[ubase + pos] = key[e];
+                if (mode) t.uni[ubase + pos] = key[e];
                 pos++;
             }
         }
         __syncthreads();
-        // row record: the row, its FP64 row sum (as FP32), its own slot, whether it is held
-        for (int i = threadIdx.x; i < T; i += blockDim.x) {
-            const int64_t gi = tile * T + i;
-            int4 ri = make_int4(-1, 0, 0, 0);
-            uint16_t self = 0;
-            if (gi < rows) {
-                const int32_t r = order[gi];
-                const int s = lower_bound_i32(uq, total, r);
-                if (s >= total || uq[s] != r) atomicOr(bad, 1);
-                self = (uint16_t)(s < total ? s : 0);
-                double acc = 0.0;
-                for (int64_t a = row_ptr[r]; a < row_ptr[r + 1]; a++) acc += val64[a];
-                ri = make_int4(r, __float_as_int((float)acc), self, (fixed && fixed[r]) ? 1 : 0);
-            }
-            selfs[i] = self;
-            t.rowinfo[gi] = ri;
-        }
-        __syncthreads();
-        // entries: slot into the union and FP32 weight; padding entries point at the row's own
-        // slot with weight 0 (their difference is exactly 0)
+        // each row's entries as union slots
         for (int e = threadIdx.x; e < T * KP; e += blockDim.x) {
             const int i = e / KP, k = e - i * KP;
             const int64_t gi = tile * T + i;
-            uint16_t slot = 0;
-            float wv = 0.0f;
+            int len = 0;
             if (gi < rows) {
                 const int32_t r = order[gi];
                 const int64_t a = row_ptr[r];
-                slot = selfs[i];
-                if (k < (int)(row_ptr[r + 1] - a)) {
-                    slot = (uint16_t)lower_bound_i32(uq, total, col[a + k]);
-                    wv = val32[a + k];
+                len = (int)(row_ptr[r + 1] - a);
+                if (k < len) {
+                    rslot[e] = (uint16_t)lower_bound_i32(uq, total, col[a + k]);
+                    rw[e] = val32[a + k];
                 }
             }
-            t.slot[tile * (int64_t)T * KP + e] = slot;
-            t.w[tile * (int64_t)T * KP + e] = wv;
+            if (k == 0) rlen[i] = len;
+        }
+        __syncthreads();
+        // merge the rows of each pair: row a's entries (with row b's weight where b has the same
+        // column), then row b's entries that row a does not have
+        for (int j = threadIdx.x; j < T / 2; j += blockDim.x) {
+            const int ia = 2 * j, ib = ia + 1;
+            const int la = rlen[ia], lb = rlen[ib];
+            const int64_t base = (tile * (T / 2) + j) * (int64_t)t.KPP;
+            int m = 0;
+            for (int ta = 0; ta < la; ta++) {
+                const uint16_t sa = rslot[ia * KP + ta];
+                float wb = 0.0f;
+                for (int tb = 0; tb < lb; tb++)
+                    if (rslot[ib * KP + tb] == sa) wb = rw[ib * KP + tb];
+                if (mode) {
+                    t.pslot[base + m] = sa;
+                    t.pw[base + m] = make_float2(rw[ia * KP + ta], wb);
+                }
+                m++;
+            }
+            for (int tb = 0; tb < lb; tb++) {
+                const uint16_t sb = rslot[ib * KP + tb];
+                bool in_a = false;
+                for (int ta = 0; ta < la; ta++) in_a |= rslot[ia * KP + ta] == sb;
+                if (in_a) continue;
+                if (mode) {
+                    t.pslot[base + m] = sb;
+                    t.pw[base + m] = make_float2(0.0f, rw[ib * KP + tb]);
+                }
+                m++;
+            }
+            if (mode == 0) {
+                atomicMax(&maxm, m);
+                continue;
+            }
+            for (int q = m; q < t.KPP; q++) {  // padding: slot 0, zero weights
+                t.pslot[base + q] = 0;
+                t.pw[base + q] = make_float2(0.0f, 0.0f);
+            }
+            // row records: the row, its FP64 row sum (as FP32), the pair's entry quads (first
+            // row), whether it is held
+            for (int h = 0; h < 2; h++) {
+                const int i = ia + h;
+                const int64_t gi = tile * T + i;
+                int4 ri = make_int4(-1, 0, 0, 0);
+                if (gi < rows) {
+                    const int32_t r = order[gi];
+                    double acc = 0.0;
+                    for (int64_t a = row_ptr[r]; a < row_ptr[r + 1]; a++) acc += val64[a];
+                    ri = make_int4(r, __float_as_int((float)acc), h == 0 ? (m + 3) >> 2 : 0,
+                                   (fixed && fixed[r]) ? 1 : 0);
+                }
+                t.rowinfo[gi] = ri;
+            }
+        }
+        __syncthreads();
+        if (mode == 0 && threadIdx.x == 0) {
+            cnt[tile] = total;
+            cnt2[tile] = maxm;
+            if (total > 65535) atomicOr(bad, 2);
         }
         __syncthreads();
     }
@@ -220,7 +258,7 @@ struct StageArgs {
 
 // The copies of one tile into `buf`, spread over all threads in 16-byte pieces: the union's
 // field rows of v, the tile's own rows of u, the tile's reference row of v (its middle row, or
-// its first when the tile is short), the weights, the slots and the row records, from the ids
+// its first when the tile is short), the merged pair entries and the row records, from the ids
 // in `ids` (a shared-memory list filled one tile ahead: U union columns, then the T rows); one
 // commit group per thread and tile.  After these land the tile is computed from shared memory.
 template <int LPR>
@@ -243,10 +281,10 @@ __device__ __forceinline__ void issue_tile(const StageArgs &s, int64_t tile, int
         if (r < 0) r = ids[U];
         cp16(buf + s.refofs + (size_t)threadIdx.x * 16, s.v + (size_t)r * F + 4 * threadIdx.x);
     }
-    const int eb = t.T * t.KP;
-    const unsigned char *wsrc = reinterpret_cast<const unsigned char *>(t.w + (size_t)tile * eb);
-    for (int c = threadIdx.x; c < eb / 4; c += blockDim.x) cp16(buf + s.wofs + (size_t)c * 16, wsrc + (size_t)c * 16);
-    const unsigned char *ssrc = reinterpret_cast<const unsigned char *>(t.slot + (size_t)tile * eb);
+    const int eb = (t.T / 2) * t.KPP;  // merged pair entries of the tile
+    const unsigned char *wsrc = reinterpret_cast<const unsigned char *>(t.pw + (size_t)tile * eb);
+    for (int c = threadIdx.x; c < eb / 2; c += blockDim.x) cp16(buf + s.wofs + (size_t)c * 16, wsrc + (size_t)c * 16);
+    const unsigned char *ssrc = reinterpret_cast<const unsigned char *>(t.pslot + (size_t)tile * eb);
     for (int c = threadIdx.x; c < eb / 8; c += blockDim.x) cp16(buf + s.sofs + (size_t)c * 16, ssrc + (size_t)c * 16);
     const int4 *rsrc = t.rowinfo + (size_t)tile * t.T;
     for (int c = threadIdx.x; c < t.T; c += blockDim.x) cp16(buf + s.rofs + (size_t)c * 16, rsrc + c);
@@ -287,8 +325,8 @@ __device__ __forceinline__ float4 f4_add(float4 a, float4 b)
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-// One stage over all tiles.  LPR = F / 4 lanes per row (one float4 of fields each), 32 / LPR rows
-// per warp and pass.  Persistent CTAs walk the tiles with a stride of gridDim.x.  Software
+// One stage over all tiles.  LPR = F / 4 lanes per row pair (one float4 of fields each), 32 / LPR
+// row pairs per warp and pass.  Persistent CTAs walk the tiles with a stride of gridDim.x.  Software
 // pipeline per tile k: issue the copies of tile k + 1 (into the other buffer, with the ids
 // stored one tile earlier), load the ids of tile k + 2 into registers, wait for this thread's
 // copies of tile k, barrier, subtract the reference row from the union rows, barrier, compute
@@ -350,38 +388,42 @@ __global__ void __launch_bounds__(512, 1) rk4_tile_stage_kernel(StageArgs s)
         __syncthreads();
         const float4 vref = ref[sl];
         const float4 *ub = reinterpret_cast<const float4 *>(buf + s.uofs);
-        const float4 *wbase = reinterpret_cast<const float4 *>(buf + s.wofs);
-        const uint2 *sbase = reinterpret_cast<const uint2 *>(buf + s.sofs);
+        const float4 *wbase = reinterpret_cast<const float4 *>(buf + s.wofs);  // 2 entries per float4
+        const uint2 *sbase = reinterpret_cast<const uint2 *>(buf + s.sofs);    // 4 slots per uint2
         const int4 *rinfo = reinterpret_cast<const int4 *>(buf + s.rofs);
-        for (int rl0 = 0; rl0 < T; rl0 += nw * RPW) {
-            const int rl = rl0 + warp * RPW + sub;
-            if (rl >= T) continue;
-            const int4 ri = rinfo[rl];
-            if (ri.x < 0) continue;
-            const float4 uo = ub[rl * LPR + sl];
-            float4 o = uo;
-            if (!ri.w) {
-                const float rs = __int_as_float(ri.y);
-                float4 acc0 = make_float4(rs * vref.x, rs * vref.y, rs * vref.z, rs * vref.w);
-                float4 acc1 = make_float4(0.f, 0.f, 0.f, 0.f);
-                const float4 *wr = wbase + rl * KQ;
-                const uint2 *sr = sbase + rl * KQ;
+        const int KQ = t.KPP >> 2;
+        for (int pj0 = 0; pj0 < T / 2; pj0 += nw * RPW) {
+            const int pj = pj0 + warp * RPW + sub;
+            if (pj >= T / 2) continue;
+            const int4 ra = rinfo[2 * pj], rb = rinfo[2 * pj + 1];
+            if (ra.x < 0) continue;
+            const float4 ua = ub[(2 * pj) * LPR + sl];
+            const float4 ubv = rb.x >= 0 ? ub[(2 * pj + 1) * LPR + sl] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float rsa = __int_as_float(ra.y), rsb = __int_as_float(rb.y);
+            float4 acca = make_float4(rsa * vref.x, rsa * vref.y, rsa * vref.z, rsa * vref.w);
+            float4 accb = make_float4(rsb * vref.x, rsb * vref.y, rsb * vref.z, rsb * vref.w);
+            const float4 *wr = wbase + pj * (2 * KQ);
+            const uint2 *sr = sbase + pj * KQ;
 #pragma unroll 2
-                for (int q = 0; q < KQ; q++) {
-                    const float4 wv = wr[q];
-                    const uint2 sv = sr[q];
-                    const float4 x0 = fb[(int)(sv.x & 0xffffu) * LPR + sl];
-                    const float4 x1 = fb[(int)(sv.x >> 16) * LPR + sl];
-                    const float4 x2 = fb[(int)(sv.y & 0xffffu) * LPR + sl];
-                    const float4 x3 = fb[(int)(sv.y >> 16) * LPR + sl];
-                    acc0 = f4_fma(wv.x, x0, acc0);
-                    acc1 = f4_fma(wv.y, x1, acc1);
-                    acc0 = f4_fma(wv.z, x2, acc0);
-                    acc1 = f4_fma(wv.w, x3, acc1);
-                }
-                o = f4_fma(s.c, f4_add(acc0, acc1), uo);
+            for (int q = 0; q < ra.z; q++) {
+                const float4 w01 = wr[2 * q], w23 = wr[2 * q + 1];  // (wa0, wb0, wa1, wb1), (wa2, wb2, wa3, wb3)
+                const uint2 sv = sr[q];
+                const float4 x0 = fb[(int)(sv.x & 0xffffu) * LPR + sl];
+                const float4 x1 = fb[(int)(sv.x >> 16) * LPR + sl];
+                const float4 x2 = fb[(int)(sv.y & 0xffffu) * LPR + sl];
+                const float4 x3 = fb[(int)(sv.y >> 16) * LPR + sl];
+                acca = f4_fma(w01.x, x0, acca);
+                accb = f4_fma(w01.y, x0, accb);
+                acca = f4_fma(w01.z, x1, acca);
+                accb = f4_fma(w01.w, x1, accb);
+                acca = f4_fma(w23.x, x2, acca);
+                accb = f4_fma(w23.y, x2, accb);
+                acca = f4_fma(w23.z, x3, acca);
+                accb = f4_fma(w23.w, x3, accb);
             }
-            reinterpret_cast<float4 *>(s.out)[(int64_t)ri.x * LPR + sl] = o;
+            float4 *out = reinterpret_cast<float4 *>(s.out);
+            out[(int64_t)ra.x * LPR + sl] = ra.w ? ua : f4_fma(s.c, acca, ua);
+            if (rb.x >= 0) out[(int64_t)rb.x * LPR + sl] = rb.w ? ubv : f4_fma(s.c, accb, ubv);
         }
         if (n2 < t.ntile) {
             pre.store(t, idsp(b));
@@ -399,8 +441,8 @@ void stage_layout(const TileOp &t, int F, StageArgs &s)
 {
     auto up128 = [](uint32_t b) { return (b + 127u) & ~127u; };
     s.wofs = up128((uint32_t)t.ucap * (uint32_t)F * 4u);
-    s.sofs = s.wofs + up128((uint32_t)t.T * t.KP * 4u);
-    s.rofs = s.sofs + up128((uint32_t)t.T * t.KP * 2u);
+    s.sofs = s.wofs + up128((uint32_t)(t.T / 2) * t.KPP * 8u);
+    s.rofs = s.sofs + up128((uint32_t)(t.T / 2) * t.KPP * 2u);
     s.uofs = s.rofs + up128((uint32_t)t.T * 16u);
     s.refofs = s.uofs + up128((uint32_t)t.T * (uint32_t)F * 4u);
     s.idofs = s.refofs + up128((uint32_t)F * 4u);
@@ -414,21 +456,26 @@ int build_keys(const TileOp &t)
     return P;
 }
 
+size_t build_smem(const TileOp &t)
+{
+    return (size_t)2 * build_keys(t) * sizeof(int32_t) + (size_t)t.T * t.KP * (sizeof(float) + sizeof(uint16_t)) + 16;
+}
+
 }  // namespace
 
 cudaError_t launch_tile_build(TileOp &t, int64_t rows, const int32_t *order, const int64_t *row_ptr,
                               const int32_t *col, const float *val32, const double *val64, const uint8_t *fixed,
-                              int mode, int32_t *cnt, int *bad, int num_sms, cudaStream_t st)
+                              int mode, int32_t *cnt, int32_t *cnt2, int *bad, int num_sms, cudaStream_t st)
 {
-    if (t.T > 256) return cudaErrorInvalidValue;
+    if (t.T > 256 || (t.T & 1)) return cudaErrorInvalidValue;
     const int P = build_keys(t);
-    const size_t smem = (size_t)2 * P * sizeof(int32_t);
+    const size_t smem = build_smem(t);
     cudaError_t e = cudaFuncSetAttribute(tile_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int64_t blocks = t.ntile < (int64_t)num_sms * 8 ? t.ntile : (int64_t)num_sms * 8;
     if (blocks < 1) blocks = 1;
     tile_build_kernel<<<(int)blocks, 256, smem, st>>>(t, rows, order, row_ptr, col, val32, val64, fixed, P, mode, cnt,
-                                                     bad);
+                                                     cnt2, bad);
     return cudaGetLastError();
 }
 
