@@ -94,7 +94,8 @@ typedef struct {
     int64_t n_rows;         /* operator rows (evaluation points) */
     int64_t n_fallback;     /* mixed: systems re-solved in FP64 */
     int64_t first_bad_node; /* 0-based X node of the first singular system, -1 if none */
-    int64_t refine_hist[8]; /* mixed: systems that converged after i refinement steps */
+    int64_t refine_hist[8]; /* mixed: systems that converged after i refinement steps (i = 0:
+                               solved directly in FP64, a class the autotuner timed faster so) */
     int64_t nnz;            /* nonzeros per operator */
     int64_t kernel_launches;/* CUDA kernels this call launched */
 } rbffd_stats;

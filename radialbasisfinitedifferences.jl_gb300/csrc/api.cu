@@ -819,11 +819,14 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     }
     {
         unsigned long long *claim;
+        int32_t *sample_list;
         CK(tmp.zeros(&claim, launches.size()));
+        CK(tmp.get(&sample_list, tune_sample_systems(h->num_sms)));
         for (size_t i = 0; i < launches.size(); i++) launches[i].next_sys = claim + i;
         std::vector<SolveConfig> cfg(launches.size());
         for (size_t i = 0; i < launches.size(); i++)
-            CK(h->tuner.choose(launches[i], table, pb->precision, h->opt.warps_per_block, h->num_sms, st, &cfg[i]));
+            CK(h->tuner.choose(launches[i], table, pb->precision, h->opt.warps_per_block, h->num_sms, sample_list, st,
+                               &cfg[i]));
         if (launches.size() == 1 || !RBFFD_CLASS_CONCURRENT) {
             for (size_t i = 0; i < launches.size(); i++)
                 CK(launch_solve_config(launches[i], table, cfg[i], h->num_sms, st));

@@ -261,22 +261,22 @@ struct StageArgs {
 // its first when the tile is short), the merged pair entries and the row records, from the ids
 // in `ids` (a shared-memory list filled one tile ahead: U union columns, then the T rows); one
 // commit group per thread and tile.  After these land the tile is computed from shared memory.
-template <int LPR>
+template <int F>
 __device__ __forceinline__ void issue_tile(const StageArgs &s, int64_t tile, int U, const int32_t *ids,
                                            unsigned char *buf)
 {
-    constexpr int F = 4 * LPR;
+    constexpr int Q4 = F / 4;  // 16-byte pieces per field row
     const TileOp &t = s.t;
-    for (int c = threadIdx.x; c < U * LPR; c += blockDim.x) {
-        const int row = c / LPR, part = c % LPR;
+    for (int c = threadIdx.x; c < U * Q4; c += blockDim.x) {
+        const int row = c / Q4, part = c % Q4;
         cp16(buf + (size_t)c * 16, s.v + (size_t)ids[row] * F + 4 * part);
     }
-    for (int c = threadIdx.x; c < t.T * LPR; c += blockDim.x) {
-        const int row = c / LPR, part = c % LPR;
+    for (int c = threadIdx.x; c < t.T * Q4; c += blockDim.x) {
+        const int row = c / Q4, part = c % Q4;
         const int32_t r = ids[U + row];
         if (r >= 0) cp16(buf + s.uofs + (size_t)c * 16, s.u + (size_t)r * F + 4 * part);
     }
-    if ((int)threadIdx.x < LPR) {
+    if ((int)threadIdx.x < Q4) {
         int32_t r = ids[U + t.T / 2];
         if (r < 0) r = ids[U];
         cp16(buf + s.refofs + (size_t)threadIdx.x * 16, s.v + (size_t)r * F + 4 * threadIdx.x);
@@ -324,28 +324,46 @@ __device__ __forceinline__ float4 f4_add(float4 a, float4 b)
 {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
+__device__ __forceinline__ float4 f4_shfl_xor(float4 a, int off)
+{
+    return make_float4(__shfl_xor_sync(RBFFD_FULL, a.x, off), __shfl_xor_sync(RBFFD_FULL, a.y, off),
+                       __shfl_xor_sync(RBFFD_FULL, a.z, off), __shfl_xor_sync(RBFFD_FULL, a.w, off));
+}
 
-// One stage over all tiles.  LPR = F / 4 lanes per row pair (one float4 of fields each), 32 / LPR
-// row pairs per warp and pass.  Persistent CTAs walk the tiles with a stride of gridDim.x.  Software
-// pipeline per tile k: issue the copies of tile k + 1 (into the other buffer, with the ids
-// stored one tile earlier), load the ids of tile k + 2 into registers, wait for this thread's
-// copies of tile k, barrier, subtract the reference row from the union rows, barrier, compute
-// tile k from shared memory, store the ids of tile k + 2, barrier.
+// How the lanes of a warp share a tile's row pairs at F fields: each half-warp (16 lanes) takes
+// one pair; in it, LPR lanes cover a row's F fields with V float4s each (lane sl holds float4s
+// sl, sl + LPR, ..., so that LPR lanes read one 128-byte piece of a field row per load), and
+// SPLIT = 16 / LPR lane groups take every SPLIT-th entry quad of the pair, their partial sums
+// combined by shuffles at the end.  Two float4s per lane at F >= 64 halve the weight and slot
+// loads and the slot arithmetic per FMA and double the gathers in flight per lane.
+template <int F>
+struct StageShape {
+    static constexpr int V = F >= 64 ? 2 : 1;
+    static constexpr int LPR = F / (4 * V);
+    static constexpr int SPLIT = 16 / LPR;
+    static_assert(LPR >= 1 && LPR <= 16 && 16 % LPR == 0, "F / (4 V) lanes must divide a half-warp");
+};
+
+// One stage over all tiles.  Persistent CTAs walk the tiles with a stride of gridDim.x.
+// Software pipeline per tile k: issue the copies of tile k + 1 (into the other buffer, with the
+// ids stored one tile earlier), load the ids of tile k + 2 into registers, wait for this
+// thread's copies of tile k, barrier, subtract the reference row from the union rows, barrier,
+// compute tile k from shared memory, store the ids of tile k + 2, barrier.
 //
 // Difference form against a tile-wide reference row v_ref (a node of the tile):
 //     (L v)_i = sum_t w_t (v_{c_t} - v_ref) + s_i v_ref,   s_i = sum_t w_t (FP64 row sum),
 // equal to the plain sum in exact arithmetic; the differences of a smooth field across a tile
 // are small, so the FP32 products carry an error proportional to them instead of to |v|, and
 // the subtraction is paid once per union row and tile instead of once per entry.
-template <int LPR>
+template <int F>
 __global__ void __launch_bounds__(512, 1) rk4_tile_stage_kernel(StageArgs s)
 {
     extern __shared__ __align__(128) unsigned char ts_smem[];
-    constexpr int RPW = 32 / LPR;
+    constexpr int Q4 = F / 4, V = StageShape<F>::V, LPR = StageShape<F>::LPR, SPLIT = StageShape<F>::SPLIT;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int sub = lane / LPR, sl = lane - sub * LPR;
+    const int pr = lane >> 4, g = (lane & 15) / LPR, sl = lane % LPR;
     const TileOp &t = s.t;
-    const int T = t.T, KQ = t.KP >> 2;
+    const int T = t.T, KQ = t.KPP >> 2;
     const int64_t G = gridDim.x;
     int64_t tile = blockIdx.x;
     if (tile >= t.ntile) return;
@@ -365,13 +383,13 @@ __global__ void __launch_bounds__(512, 1) rk4_tile_stage_kernel(StageArgs s)
         }
     }
     __syncthreads();
-    issue_tile<LPR>(s, tile, U0, idsp(0), bufp(0));
+    issue_tile<F>(s, tile, U0, idsp(0), bufp(0));
     for (int k = 0; tile < t.ntile; k++, tile += G) {
         const int b = k & 1;
         unsigned char *buf = bufp(b);
         const int U = b ? U1 : U0;
         const int64_t nxt = tile + G, n2 = nxt + G;
-        if (nxt < t.ntile) issue_tile<LPR>(s, nxt, b ? U0 : U1, idsp(b ^ 1), bufp(b ^ 1));
+        if (nxt < t.ntile) issue_tile<F>(s, nxt, b ? U0 : U1, idsp(b ^ 1), bufp(b ^ 1));
         TileIds pre;
         if (n2 < t.ntile) pre.load(t, n2);
         if (nxt < t.ntile)
@@ -382,48 +400,108 @@ __global__ void __launch_bounds__(512, 1) rk4_tile_stage_kernel(StageArgs s)
         float4 *fb = reinterpret_cast<float4 *>(buf);
         const float4 *ref = reinterpret_cast<const float4 *>(buf + s.refofs);
         {
-            const float4 rv = ref[threadIdx.x % LPR];  // blockDim is a multiple of LPR
-            for (int c = threadIdx.x; c < U * LPR; c += blockDim.x) fb[c] = f4_sub(fb[c], rv);
+            const float4 rv = ref[threadIdx.x % Q4];  // blockDim is a multiple of Q4
+            for (int c = threadIdx.x; c < U * Q4; c += blockDim.x) fb[c] = f4_sub(fb[c], rv);
         }
         __syncthreads();
-        const float4 vref = ref[sl];
+        float4 vref[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) vref[v] = ref[v * LPR + sl];
+        const float4 *fbl = fb + sl;
         const float4 *ub = reinterpret_cast<const float4 *>(buf + s.uofs);
         const float4 *wbase = reinterpret_cast<const float4 *>(buf + s.wofs);  // 2 entries per float4
         const uint2 *sbase = reinterpret_cast<const uint2 *>(buf + s.sofs);    // 4 slots per uint2
         const int4 *rinfo = reinterpret_cast<const int4 *>(buf + s.rofs);
-        const int KQ = t.KPP >> 2;
-        for (int pj0 = 0; pj0 < T / 2; pj0 += nw * RPW) {
-            const int pj = pj0 + warp * RPW + sub;
-            if (pj >= T / 2) continue;
-            const int4 ra = rinfo[2 * pj], rb = rinfo[2 * pj + 1];
-            if (ra.x < 0) continue;
-            const float4 ua = ub[(2 * pj) * LPR + sl];
-            const float4 ubv = rb.x >= 0 ? ub[(2 * pj + 1) * LPR + sl] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float rsa = __int_as_float(ra.y), rsb = __int_as_float(rb.y);
-            float4 acca = make_float4(rsa * vref.x, rsa * vref.y, rsa * vref.z, rsa * vref.w);
-            float4 accb = make_float4(rsb * vref.x, rsb * vref.y, rsb * vref.z, rsb * vref.w);
-            const float4 *wr = wbase + pj * (2 * KQ);
-            const uint2 *sr = sbase + pj * KQ;
+        for (int pj0 = 0; pj0 < T / 2; pj0 += 2 * nw) {
+            // every lane of the warp reaches the shuffles below: no early exit per pair
+            const int pj = pj0 + 2 * warp + pr;
+            const bool live = pj < T / 2;
+            const int4 ra = live ? rinfo[2 * pj] : make_int4(-1, 0, 0, 0);
+            const int4 rb = live ? rinfo[2 * pj + 1] : make_int4(-1, 0, 0, 0);
+            const int nq = ra.x >= 0 ? ra.z : 0;
+            const float rsa = g == 0 ? __int_as_float(ra.y) : 0.0f, rsb = g == 0 ? __int_as_float(rb.y) : 0.0f;
+            float4 acca[V], accb[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                acca[v] = make_float4(rsa * vref[v].x, rsa * vref[v].y, rsa * vref[v].z, rsa * vref[v].w);
+                accb[v] = make_float4(rsb * vref[v].x, rsb * vref[v].y, rsb * vref[v].z, rsb * vref[v].w);
+            }
+            const float4 *wr = wbase + (live ? pj : 0) * (2 * KQ);
+            const uint2 *sr = sbase + (live ? pj : 0) * KQ;
 #pragma unroll 2
-            for (int q = 0; q < ra.z; q++) {
+            for (int q = g; q < nq; q += SPLIT) {
                 const float4 w01 = wr[2 * q], w23 = wr[2 * q + 1];  // (wa0, wb0, wa1, wb1), (wa2, wb2, wa3, wb3)
                 const uint2 sv = sr[q];
-                const float4 x0 = fb[(int)(sv.x & 0xffffu) * LPR + sl];
-                const float4 x1 = fb[(int)(sv.x >> 16) * LPR + sl];
-                const float4 x2 = fb[(int)(sv.y & 0xffffu) * LPR + sl];
-                const float4 x3 = fb[(int)(sv.y >> 16) * LPR + sl];
-                acca = f4_fma(w01.x, x0, acca);
-                accb = f4_fma(w01.y, x0, accb);
-                acca = f4_fma(w01.z, x1, acca);
-                accb = f4_fma(w01.w, x1, accb);
-                acca = f4_fma(w23.x, x2, acca);
-                accb = f4_fma(w23.y, x2, accb);
-                acca = f4_fma(w23.z, x3, acca);
-                accb = f4_fma(w23.w, x3, accb);
+                const float4 *p0 = fbl + (sv.x & 0xffffu) * Q4, *p1 = fbl + (sv.x >> 16) * Q4;
+                const float4 *p2 = fbl + (sv.y & 0xffffu) * Q4, *p3 = fbl + (sv.y >> 16) * Q4;
+                float4 x0[V], x1[V], x2[V], x3[V];
+#pragma unroll
+                for (int v = 0; v < V; v++) {
+                    x0[v] = p0[v * LPR];
+                    x1[v] = p1[v * LPR];
+                    x2[v] = p2[v * LPR];
+                    x3[v] = p3[v * LPR];
+                }
+#pragma unroll
+                for (int v = 0; v < V; v++) {
+                    acca[v] = f4_fma(w01.x, x0[v], acca[v]);
+                    accb[v] = f4_fma(w01.y, x0[v], accb[v]);
+                    acca[v] = f4_fma(w01.z, x1[v], acca[v]);
+                    accb[v] = f4_fma(w01.w, x1[v], accb[v]);
+                    acca[v] = f4_fma(w23.x, x2[v], acca[v]);
+                    accb[v] = f4_fma(w23.y, x2[v], accb[v]);
+                    acca[v] = f4_fma(w23.z, x3[v], acca[v]);
+                    accb[v] = f4_fma(w23.w, x3[v], accb[v]);
+                }
             }
-            float4 *out = reinterpret_cast<float4 *>(s.out);
-            out[(int64_t)ra.x * LPR + sl] = ra.w ? ua : f4_fma(s.c, acca, ua);
-            if (rb.x >= 0) out[(int64_t)rb.x * LPR + sl] = rb.w ? ubv : f4_fma(s.c, accb, ubv);
+            float4 *outp = reinterpret_cast<float4 *>(s.out);
+            if constexpr (SPLIT == 1) {
+                if (ra.x >= 0) {
+                    const float4 *ur = ub + (2 * pj) * Q4 + sl;
+                    float4 *o = outp + (int64_t)ra.x * Q4 + sl;
+#pragma unroll
+                    for (int v = 0; v < V; v++) {
+                        const float4 uu = ur[v * LPR];
+                        o[v * LPR] = ra.w ? uu : f4_fma(s.c, acca[v], uu);
+                    }
+                }
+                if (rb.x >= 0) {
+                    const float4 *ur = ub + (2 * pj + 1) * Q4 + sl;
+                    float4 *o = outp + (int64_t)rb.x * Q4 + sl;
+#pragma unroll
+                    for (int v = 0; v < V; v++) {
+                        const float4 uu = ur[v * LPR];
+                        o[v * LPR] = rb.w ? uu : f4_fma(s.c, accb[v], uu);
+                    }
+                }
+            } else {
+                // sum the SPLIT groups' partials: butterfly over all but the lowest group bit,
+                // then one exchange in which even groups keep row a and odd groups row b
+#pragma unroll
+                for (int off = 8; off >= 2 * LPR; off >>= 1)
+#pragma unroll
+                    for (int v = 0; v < V; v++) {
+                        acca[v] = f4_add(acca[v], f4_shfl_xor(acca[v], off));
+                        accb[v] = f4_add(accb[v], f4_shfl_xor(accb[v], off));
+                    }
+                const bool odd = g & 1;
+                float4 mine[V];
+#pragma unroll
+                for (int v = 0; v < V; v++) {
+                    const float4 other = f4_shfl_xor(odd ? acca[v] : accb[v], LPR);
+                    mine[v] = f4_add(odd ? accb[v] : acca[v], other);
+                }
+                const int4 r = odd ? rb : ra;
+                if (g < 2 && r.x >= 0) {
+                    const float4 *ur = ub + (2 * pj + g) * Q4 + sl;
+                    float4 *o = outp + (int64_t)r.x * Q4 + sl;
+#pragma unroll
+                    for (int v = 0; v < V; v++) {
+                        const float4 uu = ur[v * LPR];
+                        o[v * LPR] = r.w ? uu : f4_fma(s.c, mine[v], uu);
+                    }
+                }
+            }
         }
         if (n2 < t.ntile) {
             pre.store(t, idsp(b));
@@ -493,12 +571,12 @@ cudaError_t tile_stage_prepare(const TileOp &t, int F)
     const int smem = (int)tile_stage_smem(t, F);
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     switch (F) {
-    case 4: return cudaFuncSetAttribute(rk4_tile_stage_kernel<1>, a, smem);
-    case 8: return cudaFuncSetAttribute(rk4_tile_stage_kernel<2>, a, smem);
-    case 16: return cudaFuncSetAttribute(rk4_tile_stage_kernel<4>, a, smem);
-    case 32: return cudaFuncSetAttribute(rk4_tile_stage_kernel<8>, a, smem);
-    case 64: return cudaFuncSetAttribute(rk4_tile_stage_kernel<16>, a, smem);
-    case 128: return cudaFuncSetAttribute(rk4_tile_stage_kernel<32>, a, smem);
+    case 4: return cudaFuncSetAttribute(rk4_tile_stage_kernel<4>, a, smem);
+    case 8: return cudaFuncSetAttribute(rk4_tile_stage_kernel<8>, a, smem);
+    case 16: return cudaFuncSetAttribute(rk4_tile_stage_kernel<16>, a, smem);
+    case 32: return cudaFuncSetAttribute(rk4_tile_stage_kernel<32>, a, smem);
+    case 64: return cudaFuncSetAttribute(rk4_tile_stage_kernel<64>, a, smem);
+    case 128: return cudaFuncSetAttribute(rk4_tile_stage_kernel<128>, a, smem);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -517,12 +595,12 @@ cudaError_t launch_tile_stage(const TileOp &t, const float *v, const float *u, f
     const size_t smem = (size_t)2 * s.bufbytes;
     const int blocks = (int)(t.ntile < (int64_t)num_sms ? t.ntile : (int64_t)num_sms);
     switch (F) {
-    case 4: rk4_tile_stage_kernel<1><<<blocks, 512, smem, st>>>(s); break;
-    case 8: rk4_tile_stage_kernel<2><<<blocks, 512, smem, st>>>(s); break;
-    case 16: rk4_tile_stage_kernel<4><<<blocks, 512, smem, st>>>(s); break;
-    case 32: rk4_tile_stage_kernel<8><<<blocks, 512, smem, st>>>(s); break;
-    case 64: rk4_tile_stage_kernel<16><<<blocks, 512, smem, st>>>(s); break;
-    case 128: rk4_tile_stage_kernel<32><<<blocks, 512, smem, st>>>(s); break;
+    case 4: rk4_tile_stage_kernel<4><<<blocks, 512, smem, st>>>(s); break;
+    case 8: rk4_tile_stage_kernel<8><<<blocks, 512, smem, st>>>(s); break;
+    case 16: rk4_tile_stage_kernel<16><<<blocks, 512, smem, st>>>(s); break;
+    case 32: rk4_tile_stage_kernel<32><<<blocks, 512, smem, st>>>(s); break;
+    case 64: rk4_tile_stage_kernel<64><<<blocks, 512, smem, st>>>(s); break;
+    case 128: rk4_tile_stage_kernel<128><<<blocks, 512, smem, st>>>(s); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -37,15 +37,10 @@ namespace {
 
 constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never updated
 
-// Resident CTAs of 4 warps per SM requested for stencils of <= 32 nodes (4: <= 128 registers
-// per thread, 16 warps per SM) and of 33..48 nodes (2: the 2 x 48 register-resident Phi^-1
-// entries fit without spills).
-#ifndef RBFFD_SCHUR_MIN_BLOCKS
-#define RBFFD_SCHUR_MIN_BLOCKS 4
-#endif
-#ifndef RBFFD_SCHUR48_MIN_BLOCKS
-#define RBFFD_SCHUR48_MIN_BLOCKS 2
-#endif
+// Register budget: 16 resident warps per SM for stencils of <= 32 nodes (<= 128 registers per
+// thread) and 8 for larger ones (the 2 x 48 or 2 x 64 register-resident Phi^-1 entries of a
+// lane need up to 255).  A CTA may hold all of an SM's warps (512 or 256 threads).
+#define RBFFD_SCHUR_MAX_THREADS(SP) ((SP) <= 32 ? 512 : 256)
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
 template <int B, int E, typename F>
@@ -919,10 +914,20 @@ __device__ __forceinline__ void write_row_df(const SolveArgs &a, const OpTable &
     }
 }
 
+// Systems are claimed from a counter, a CTA's warps together: at a CTA barrier one thread
+// takes the next wpb systems for the CTA's wpb warps, so that the warps of a CTA start every
+// system at the same time.  The kernel is large (the elimination, the Schur complement and the
+// residuals are unrolled over compile-time register indices), and warps that drift apart -- as
+// they do when systems need different numbers of refinement steps -- run different parts of it
+// at once, which an SM's instruction cache cannot hold: on 45-node stencils with degree 4 (a
+// quarter of the systems needing one more step than the rest) the free-running kernel spent
+// 18 warp-cycles per issued instruction waiting for instructions and ran at 510 ns per system
+// against 180-240 ns while its warps were still in step.  Without a counter (a.next_sys null)
+// warps take systems by a fixed grid stride.
 template <int SP, int SM, int RMAX>
-__global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : (SP <= 48 ? RBFFD_SCHUR48_MIN_BLOCKS : 2)))
-    solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
+__global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_schur_kernel(SolveArgs a, OpTable ops)
 {
+    __shared__ unsigned long long cta_claim;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const SchurLayout L = make_schur_layout(SP, SM, a.max_n, a.max_m, ops.nops);
@@ -960,15 +965,22 @@ __global__ void __launch_bounds__(128, (SP <= 32 ? RBFFD_SCHUR_MIN_BLOCKS : (SP 
 
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    // Systems are claimed from a counter when one is given (warps that start late -- behind
-    // kernels of another stream -- then simply take fewer), else by a fixed grid stride.
-    auto next = [&](int64_t cur) -> int64_t {
-        if (!a.next_sys) return cur + nw;
-        unsigned long long v = 0ull;
-        if (lane == 0) v = atomicAdd(a.next_sys, 1ull);
-        return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
-    };
-    for (int64_t ts = a.next_sys ? next(0) : gw; ts < a.nsys; ts = next(ts)) {
+    const bool claim = a.next_sys != nullptr;
+    const int wpb = blockDim.x >> 5;
+    int64_t ts = gw - nw;
+    for (;;) {
+        if (claim) {
+            __syncthreads();  // every warp of the CTA is done with its previous system
+            if (threadIdx.x == 0) cta_claim = atomicAdd(a.next_sys, (unsigned long long)wpb);
+            __syncthreads();
+            const int64_t first = (int64_t)cta_claim;
+            if (first >= a.nsys) break;  // uniform over the CTA
+            ts = first + wib;
+            if (ts >= a.nsys) continue;  // no system for this warp in the last round
+        } else {
+            ts += nw;
+            if (ts >= a.nsys) break;
+        }
         const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
         const int j = a.sys_node[sys];
         const int n = a.n_node ? a.n_node[j] : a.n;
@@ -1090,8 +1102,12 @@ cudaError_t launch_schur(const SolveArgs &a, const OpTable &ops, int wpb, int nu
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     while (wpb > 1 && per_warp * wpb > (size_t)smem_max) wpb--;
     if (per_warp * wpb > (size_t)smem_max) return cudaErrorNotSupported;
-    const size_t smem = per_warp * wpb;
     auto kern = solve_mixed_schur_kernel<SP, SM, RMAX>;
+    cudaFuncAttributes fa;
+    cudaError_t ea = cudaFuncGetAttributes(&fa, kern);
+    if (ea != cudaSuccess) return ea;
+    while (wpb > 1 && wpb * 32 > fa.maxThreadsPerBlock) wpb--;
+    const size_t smem = per_warp * wpb;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;

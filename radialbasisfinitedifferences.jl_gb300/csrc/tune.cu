@@ -5,9 +5,14 @@
 // spent, and which one wins depends on the class: the register Schur kernel (mixed precision,
 // n <= 64, m <= 32, at most 8 operators) against the shared-memory mixed kernel, and the warps
 // per CTA of each (the per-warp shared memory grows with s = n + m, so a wide CTA can leave an
-// SM's shared memory partly unused).  Each candidate is launched once on a few warm-up systems
-// (module load) and then timed with CUDA events on the first `sample` systems of the class;
-// the fastest is cached on the handle for that class, so later builds pay nothing.
+// SM's shared memory partly unused).  In mixed precision the FP64 kernel is a candidate too: a
+// class of ill-conditioned systems (PHS r^5 with high-degree polynomials) can need so many
+// refinement steps that solving it directly in FP64 is faster, and its weights are at least as
+// accurate.  Each candidate is launched once on a few warm-up systems (module load) and then
+// timed with CUDA events on `sample` systems spread evenly over the class (the first systems of
+// a class are the nodes of one edge of the domain, whose conditioning is not the class's); the
+// fastest is cached on the handle for that class, so later builds pay nothing.
+#include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -47,11 +52,17 @@ std::vector<SolveConfig> candidates(const SolveArgs &a, const OpTable &t, int pr
             if (pw * w <= cap) c.push_back({SOLVE_KERNEL_FP64, w});
         return c;
     }
+    // the Schur kernel starts a CTA's systems together (instruction-cache locality), so its
+    // candidates are CTAs of several warps, up to all of an SM's resident warps
     if (schur_eligible(a, t))
-        for (int w : {1, 2, 4}) c.push_back({SOLVE_KERNEL_SCHUR, w});
+        for (int w : {4, 8, 16})
+            if (w <= (a.max_n <= 32 ? 16 : 8)) c.push_back({SOLVE_KERNEL_SCHUR, w});
     const size_t pw = solve_mixed_smem_per_warp(a.max_s, a.max_n, t.nops);
     for (int w : {1, 2, 4, 8})
         if (pw * w <= cap) c.push_back({SOLVE_KERNEL_SMEM_MIXED, w});
+    const size_t pf = solve_fp64_smem_per_warp(a.max_s, a.max_n, t.nops);
+    for (int w : {1, 2, 4, 8})
+        if (pf * w <= cap) c.push_back({SOLVE_KERNEL_FP64, w});
     return c;
 }
 
@@ -61,9 +72,19 @@ SolveConfig heuristic(const SolveArgs &a, const OpTable &t, int precision, int f
         const int w = fixed_wpb > 0 ? fixed_wpb : heuristic_wpb(solve_fp64_smem_per_warp(a.max_s, a.max_n, t.nops));
         return {SOLVE_KERNEL_FP64, w};
     }
-    if (schur_eligible(a, t)) return {SOLVE_KERNEL_SCHUR, fixed_wpb > 0 && fixed_wpb <= 4 ? fixed_wpb : 4};
+    if (schur_eligible(a, t)) return {SOLVE_KERNEL_SCHUR, fixed_wpb > 0 && fixed_wpb <= 16 ? fixed_wpb : 4};
     const int w = fixed_wpb > 0 ? fixed_wpb : heuristic_wpb(solve_mixed_smem_per_warp(a.max_s, a.max_n, t.nops));
     return {SOLVE_KERNEL_SMEM_MIXED, w};
+}
+
+// out[i] = the class's system at position floor(i * nsys / sample) (list[...] when the class is a
+// list of systems, the position itself otherwise).
+__global__ void sample_list_kernel(const int32_t *list, int64_t nsys, int64_t sample, int32_t *out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= sample) return;
+    const int64_t pos = i * nsys / sample;
+    out[i] = list ? list[pos] : (int32_t)pos;
 }
 
 const char *kernel_name(int k)
@@ -83,7 +104,7 @@ cudaError_t launch_solve_config(const SolveArgs &a, const OpTable &t, SolveConfi
 }
 
 cudaError_t SolveTuner::choose(const SolveArgs &a, const OpTable &t, int precision, int fixed_wpb, int num_sms,
-                               cudaStream_t st, SolveConfig *out)
+                               int32_t *sample_list, cudaStream_t st, SolveConfig *out)
 {
     const int collocated = a.Y == nullptr;
     for (const TuneRecord &r : cache_)
@@ -94,13 +115,17 @@ cudaError_t SolveTuner::choose(const SolveArgs &a, const OpTable &t, int precisi
         }
     TuneRecord rec{precision, a.max_n, a.max_m, t.nops, t.p, a.unscaled_overload, collocated, {}, false, 0, {}, {}};
     // enough systems to fill every SM a few times over
-    const int64_t sample = (int64_t)num_sms * 64;
+    const int64_t sample = tune_sample_systems(num_sms);
     std::vector<SolveConfig> cand = candidates(a, t, precision);
-    if (fixed_wpb > 0 || a.nsys < 3 * sample || cand.size() < 2 || !a.next_sys) {
+    if (fixed_wpb > 0 || a.nsys < 3 * sample || a.nsys > INT32_MAX || cand.size() < 2 || !a.next_sys ||
+        !sample_list) {
         // a small class is not cached: a later, larger class of the same shape may be timed
         *out = heuristic(a, t, precision, fixed_wpb);
         return cudaSuccess;
     }
+    sample_list_kernel<<<(unsigned)((sample + 255) / 256), 256, 0, st>>>(a.sys_list, a.nsys, sample, sample_list);
+    cudaError_t lerr = cudaGetLastError();
+    if (lerr != cudaSuccess) return lerr;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -109,6 +134,7 @@ cudaError_t SolveTuner::choose(const SolveArgs &a, const OpTable &t, int precisi
     cudaError_t err = cudaSuccess;
     for (const SolveConfig &c : cand) {
         SolveArgs s = a;
+        s.sys_list = sample_list;
         s.nsys = 32;  // warm-up: module load and first-launch costs stay out of the timing
         if ((err = cudaMemsetAsync(a.next_sys, 0, sizeof(unsigned long long), st)) != cudaSuccess) break;
         err = launch_solve_config(s, t, c, num_sms, st);

@@ -92,6 +92,9 @@ __global__ void __launch_bounds__(256) solve_fp64_kernel(SolveArgs a, OpTable op
             write_row(a, ops, row, B, n, sid, sx, sy, lane);
             __syncwarp();
         }
+        // a mixed-precision build whose class the autotuner gave to this kernel: the system
+        // needed no refinement step
+        if (a.hist && !subset && lane == 0) atomicAdd(&a.hist[0], 1ull);
     }
 }
 
@@ -219,10 +222,20 @@ __global__ void __launch_bounds__(256) solve_mixed_kernel(SolveArgs a, OpTable o
     }
 }
 
+// Grid of a persistent launch: as many CTAs of wpb warps as fit on the GPU at once (fewer when
+// there is less work).  wpb is lowered until wpb warps' shared memory fits a CTA.
 template <typename K>
-cudaError_t launch_persistent(K kernel, int wpb, int num_sms, size_t smem, int64_t nwork, cudaStream_t st,
-                              int *blocks_out)
+cudaError_t launch_persistent(K kernel, int &wpb, int num_sms, size_t per_warp, int64_t nwork, cudaStream_t st,
+                              int *blocks_out, size_t *smem_out)
 {
+    int dev = 0, smem_cap = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (wpb < 1) wpb = 1;
+    while (wpb > 1 && per_warp * wpb > (size_t)smem_cap) wpb--;
+    if (per_warp * wpb > (size_t)smem_cap) return cudaErrorNotSupported;
+    const size_t smem = per_warp * wpb;
+    *smem_out = smem;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;
@@ -250,9 +263,10 @@ static cudaError_t launch_fp64_impl(const SolveArgs &a, const OpTable &ops, int 
                                     cudaStream_t st, const int32_t *subset, const int *subset_count,
                                     int64_t nwork_hint)
 {
-    size_t smem = solve_fp64_smem_per_warp(a.max_s, a.max_n, ops.nops) * wpb;
+    size_t smem = 0;
     int blocks = 0;
-    cudaError_t e = launch_persistent(solve_fp64_kernel, wpb, num_sms, smem, nwork_hint, st, &blocks);
+    cudaError_t e = launch_persistent(solve_fp64_kernel, wpb, num_sms, solve_fp64_smem_per_warp(a.max_s, a.max_n, ops.nops),
+                                      nwork_hint, st, &blocks, &smem);
     if (e != cudaSuccess) return e;
     solve_fp64_kernel<<<blocks, wpb * 32, smem, st>>>(a, ops, subset, subset_count);
     return cudaGetLastError();
@@ -274,9 +288,10 @@ cudaError_t launch_solve_fp64_subset(const SolveArgs &a, const OpTable &ops, int
 template <int NS, int RMAX>
 static cudaError_t launch_mixed_t(const SolveArgs &a, const OpTable &ops, int wpb, int num_sms, cudaStream_t st)
 {
-    size_t smem = solve_mixed_smem_per_warp(a.max_s, a.max_n, ops.nops) * wpb;
+    size_t smem = 0;
     int blocks = 0;
-    cudaError_t e = launch_persistent(solve_mixed_kernel<NS, RMAX>, wpb, num_sms, smem, a.nsys, st, &blocks);
+    cudaError_t e = launch_persistent(solve_mixed_kernel<NS, RMAX>, wpb, num_sms,
+                                      solve_mixed_smem_per_warp(a.max_s, a.max_n, ops.nops), a.nsys, st, &blocks, &smem);
     if (e != cudaSuccess) return e;
     solve_mixed_kernel<NS, RMAX><<<blocks, wpb * 32, smem, st>>>(a, ops);
     return cudaGetLastError();

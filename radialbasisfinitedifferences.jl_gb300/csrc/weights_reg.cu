@@ -33,7 +33,7 @@ cudaError_t launch_solve_mixed_reg(const SolveArgs &a, const OpTable &ops, int m
     if (a.nsys <= 0) return cudaSuccess;
     const int r = ops.nops;
     if (r > 8 || a.max_n > 64 || a.max_m > 32 || a.unscaled_overload) return cudaErrorNotSupported;
-    if (wpb > 4 || wpb < 1) wpb = 4;
+    if (wpb > 16 || wpb < 1) wpb = 4;  // launch_schur lowers it to what the kernel and shared memory allow
     const int SM = a.max_m <= 16 ? 16 : 32;
     const int RMAX = r <= 4 ? 4 : 8;
     if (a.max_n <= 32) return launch_schur_sp32(a, ops, SM, RMAX, wpb, num_sms, st);

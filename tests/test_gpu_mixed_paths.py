@@ -172,3 +172,18 @@ def test_generic_mixed_kernel_forced_fallback(pkg, orc, gpu):
         with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision="mixed", handle=h) as s:
             assert s.stats.n_fallback == len(X)
             check_against_oracle(s, ref, ops, n, MIXED_TOL)
+
+
+@pytest.mark.parametrize("wpb", [8, 16])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_fixed_cta_size_beyond_shared_memory(pkg, orc, gpu, wpb, precision):
+    """A fixed CTA size (rbffd_options.warps_per_block) larger than a 60-node, degree-5
+    system's shared memory allows: the launches lower it to what fits instead of failing, and
+    the weights still match the oracle."""
+    X = grid(pkg, 40, seed=21)
+    p, n, deg = 3, 60, 5
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    with pkg.Handle(warps_per_block=wpb) as h:
+        with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision=precision, handle=h) as s:
+            check_against_oracle(s, ref, ops, n, HARD_TOL)
