@@ -1275,7 +1275,8 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
     }
     if (dtype == 1 && tile_stage_supported(nfields)) {
         // FP32 tile layout: tiles of 64 consecutive rows of the Z-curve order, each tile's
-        // stencil-column union, 16-bit slots (rk4_tiled.cu)
+        // stencil-column union, groups of 8 rows with dense weights over their columns
+        // (rk4_tiled.cu)
         int kmax = s0->uniform ? s0->n : 0;
         if (!s0->uniform) {
             std::vector<int64_t> hp(rk->rows + 1);
@@ -1284,49 +1285,53 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
             for (int64_t i = 0; i < rk->rows; i++) kmax = std::max<int>(kmax, (int)(hp[i + 1] - hp[i]));
         }
         TileOp t;
-        t.T = 64;
         t.KP = kmax;
-        t.ntile = (rk->rows + t.T - 1) / t.T;
-        int32_t *cnt, *cnt2;
-        int *bad;
+        t.ntile = (rk->rows + TileOp::T - 1) / TileOp::T;
+        const int64_t ngroup = t.ntile * (TileOp::T / TileOp::G);
+        int32_t *cnt, *gcnt;
         CKB(tmp.get(&cnt, t.ntile));
-        CKB(tmp.get(&cnt2, t.ntile));
-        CKB(tmp.zeros(&bad, 1));
+        CKB(tmp.get(&gcnt, ngroup));
         CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 0, cnt,
-                              cnt2, bad, h->num_sms, st));
-        std::vector<int32_t> hc(t.ntile), hc2(t.ntile);
-        int hbad = 0;
+                              gcnt, h->num_sms, st));
+        std::vector<int32_t> hc(t.ntile), hg(ngroup);
         CKB(cudaMemcpyAsync(hc.data(), cnt, sizeof(int32_t) * t.ntile, cudaMemcpyDeviceToHost, st));
-        CKB(cudaMemcpyAsync(hc2.data(), cnt2, sizeof(int32_t) * t.ntile, cudaMemcpyDeviceToHost, st));
-        CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CKB(cudaMemcpyAsync(hg.data(), gcnt, sizeof(int32_t) * ngroup, cudaMemcpyDeviceToHost, st));
         CKB(cudaStreamSynchronize(st));
-        std::vector<int32_t> hu(t.ntile + 1);
-        int64_t tot = 0;
-        int kpp = 0;
+        std::vector<int32_t> hu(t.ntile + 1), hgp(ngroup + 1);
+        int64_t tot = 0, gtot = 0;
         for (int64_t i = 0; i < t.ntile; i++) {
             hu[i] = (int32_t)tot;
             tot += hc[i];
             t.ucap = std::max(t.ucap, hc[i]);
-            kpp = std::max(kpp, hc2[i]);
+            int64_t tile_cols = 0;
+            for (int g = 0; g < TileOp::T / TileOp::G; g++) {
+                const int64_t gi = i * (TileOp::T / TileOp::G) + g;
+                hgp[gi] = (int32_t)gtot;
+                gtot += hg[gi];
+                tile_cols += hg[gi];
+            }
+            t.gcap = (int)std::max<int64_t>(t.gcap, tile_cols);
         }
         hu[t.ntile] = (int32_t)tot;
-        t.KPP = (kpp + 3) & ~3;  // whole quads of merged entries
+        hgp[ngroup] = (int32_t)gtot;
         int smem_max = 0;
         cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-        if (!hbad && tot < INT32_MAX && tile_stage_smem(t, nfields) <= (size_t)smem_max) {
-            int32_t *uptr;
+        if (tot < INT32_MAX && 8 * gtot < INT32_MAX && tile_stage_smem(t, nfields) <= (size_t)smem_max) {
+            int32_t *uptr, *gptr;
             CKB(keep.get(&uptr, t.ntile + 1));
+            CKB(keep.get(&gptr, ngroup + 1));
             CKB(keep.get(&t.uni, tot));
-            CKB(keep.get(&t.pw, (size_t)t.ntile * (t.T / 2) * t.KPP));
-            CKB(keep.get(&t.pslot, (size_t)t.ntile * (t.T / 2) * t.KPP));
-            CKB(keep.get(&t.rowinfo, (size_t)t.ntile * t.T));
+            CKB(keep.get(&t.gslot, gtot));
+            CKB(keep.get(&t.gw, 8 * gtot));
+            CKB(keep.get(&t.rowinfo, (size_t)t.ntile * TileOp::T));
             CKB(cudaMemcpyAsync(uptr, hu.data(), sizeof(int32_t) * (t.ntile + 1), cudaMemcpyHostToDevice, st));
+            CKB(cudaMemcpyAsync(gptr, hgp.data(), sizeof(int32_t) * (ngroup + 1), cudaMemcpyHostToDevice, st));
             t.uptr = uptr;
+            t.gptr = gptr;
             CKB(launch_tile_build(t, rk->rows, rk->order, rk->row_ptr, rk->col, rk->val32, rk->val64, rk->fixed, 1,
-                                  cnt, cnt2, bad, h->num_sms, st));
-            CKB(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+                                  cnt, gcnt, h->num_sms, st));
             CKB(cudaStreamSynchronize(st));
-            if (!hbad && tile_stage_prepare(t, nfields) == cudaSuccess) {
+            if (tile_stage_prepare(t, nfields) == cudaSuccess) {
                 rk->tiles = t;
                 rk->tiled = true;
             }
