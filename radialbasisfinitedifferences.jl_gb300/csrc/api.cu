@@ -1286,6 +1286,7 @@ RBFFD_EXPORT int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int
         }
         TileOp t;
         t.KP = kmax;
+        t.F = nfields;
         t.ntile = (rk->rows + TileOp::T - 1) / TileOp::T;
         const int64_t ngroup = t.ntile * (TileOp::T / TileOp::G);
         int32_t *cnt, *gcnt;

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows,
                             for (int k = 0; k < rlen[i]; k++)
                                 if (rslot[i * KP + k] == s) w8[r] = rw[i * KP + k];
                     }
-                    t.gslot[base + j] = (uint32_t)s;
+                    t.gslot[base + j] = (uint32_t)s * (uint32_t)t.F;
                     float4 *dst = reinterpret_cast<float4 *>(t.gw + (base + j) * TG);
                     dst[0] = make_float4(w8[0], w8[1], w8[2], w8[3]);
                     dst[1] = make_float4(w8[4], w8[5], w8[6], w8[7]);
@@ -332,10 +332,11 @@ __device__ __forceinline__ void st_fields(float *p, const Fv<N> &v)
 // flight while the current tile is copied and computed) and stored to shared memory when the
 // current tile's copies have been issued.  Up to three union ids per thread.
 struct TileMeta {
-    int32_t a = 0, U = 0, g0 = 0, gn = 0, gofs = 0, ref = 0;
+    int32_t a = 0, U = 0, g0 = 0, gn = 0, gofs = 0, ref = 0, row = -1;
     int32_t id[3] = {0, 0, 0};
     __device__ void load(const TileOp &t, int64_t tile)
     {
+        if ((int)threadIdx.x < TT) row = t.rowinfo[tile * TT + threadIdx.x].x;
         a = t.uptr[tile];
         U = t.uptr[tile + 1] - a;
         g0 = t.gptr[tile * NGRP];
@@ -349,8 +350,12 @@ struct TileMeta {
         ref = t.rowinfo[tile * TT + TT / 2].x;   // the tile's reference node: its middle row,
         if (ref < 0) ref = t.rowinfo[tile * TT].x;  // or its first, when the tile is short
     }
-    __device__ void store(const TileOp &t, int32_t *ids, int *goff, int *refrow) const
+    // Also starts moving the tile's rows of u (read by its epilogue) from DRAM into L2.
+    __device__ void store(const TileOp &t, int32_t *ids, int *goff, int *refrow, const float *u) const
     {
+        if (row >= 0)
+            for (int o = 0; o < t.F; o += 32)  // one 128-byte line per prefetch
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(u + (size_t)row * t.F + o));
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             const int i = threadIdx.x + q * blockDim.x;
@@ -389,7 +394,7 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : 3)) rk4_tile_stage_
     if (tile >= t.ntile) return;
     TileMeta cur;
     cur.load(t, tile);
-    cur.store(t, ids, goff, refrow);
+    cur.store(t, ids, goff, refrow, s.u);
     __syncthreads();
     for (; tile < t.ntile; tile += gridDim.x) {
         const int U = cur.U, g0 = cur.g0, gn = cur.gn;
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : 3)) rk4_tile_stage_
         if (nxt < t.ntile) cur.load(t, nxt);
         cp_wait_all();
         __syncthreads();  // the tile is in shared memory; its ids and offsets are consumed
-        if (nxt < t.ntile) cur.store(t, ids, goff, refrow);  // read after the next barrier
+        if (nxt < t.ntile) cur.store(t, ids, goff, refrow, s.u);  // read after the next barrier
         {
             const Fv<FPL> vr = ld_fields<FPL>(vref + lofs);
             float acc[TG][FPL];
@@ -425,7 +430,7 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : 3)) rk4_tile_stage_
                 const uint32_t sc[4] = {s4.x, s4.y, s4.z, s4.w};
                 Fv<FPL> x[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) x[q] = ld_fields<FPL>(fbl + (size_t)sc[q] * F);
+                for (int q = 0; q < 4; q++) x[q] = ld_fields<FPL>(fbl + sc[q]);
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const float4 wa = w4[2 * (j + q)], wb = w4[2 * (j + q) + 1];
@@ -507,7 +512,7 @@ cudaError_t launch_tile_build(TileOp &t, int64_t rows, const int32_t *order, con
                               const int32_t *col, const float *val32, const double *val64, const uint8_t *fixed,
                               int mode, int32_t *cnt, int32_t *gcnt, int num_sms, cudaStream_t st)
 {
-    if (t.KP < 1) return cudaErrorInvalidValue;
+    if (t.KP < 1 || !tile_stage_supported(t.F)) return cudaErrorInvalidValue;
     const int P = pow2_at_least(TT * t.KP, 256), PG = pow2_at_least(TG * t.KP, 32);
     const size_t smem = build_smem(t, P, PG);
     cudaError_t e = cudaFuncSetAttribute(tile_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -546,6 +551,7 @@ cudaError_t launch_tile_stage(const TileOp &t, const float *v, const float *u, f
                               int num_sms, cudaStream_t st)
 {
     if (t.ntile <= 0) return cudaSuccess;
+    if (F != t.F) return cudaErrorInvalidValue;  // the layout's offsets are for t.F fields
     if (t.ctas_per_sm < 1) return cudaErrorInvalidConfiguration;  // tile_stage_prepare not run
     StageArgs s{};
     s.t = t;

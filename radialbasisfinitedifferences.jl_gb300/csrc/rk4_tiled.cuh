@@ -6,8 +6,9 @@
 
 // Rows grouped into tiles of T = 64 consecutive rows of the RK4 row order (a Z-curve order of
 // the nodes), each tile into 8 groups of G = 8 consecutive rows.  Per tile: the sorted distinct
-// stencil columns (the union, uptr/uni).  Per group: its distinct columns as slots into the
-// tile's union (gslot, sorted, padded with slot 0 to a multiple of 4) and, for each of them,
+// stencil columns (the union, uptr/uni).  Per group: its distinct columns as positions of their
+// field rows in the tile's staged union (gslot = slot * F, sorted, padded with slot 0 to a
+// multiple of 4) and, for each of them,
 // the FP32 weights of the group's 8 rows (gw, 8 floats per column, 0 where a row does not use
 // the column).  gptr[ntile * 8 + 1]: the groups' first columns, consecutive groups adjacent.
 // rowinfo, one 16-byte record per position of the row order (padded to ntile * T): x = the row
@@ -16,6 +17,7 @@
 // tile.
 struct TileOp {
     static constexpr int T = 64, G = 8;
+    int F = 0;  // fields per row (the staged union rows' stride)
     int KP = 0;
     int64_t ntile = 0;
     int ucap = 0, gcap = 0;
