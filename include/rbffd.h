@@ -225,8 +225,9 @@ int rbffd_spmm(rbffd_handle *h, rbffd_opset *s, int op, const void *x, void *y, 
    1: FP32.  Fields are row-major [rows][nfields] device arrays.  FP32 with nfields in
    {4, 8, 16, 32, 64, 128} applies L tile by tile from shared memory (tiles of 64 rows of a
    Z-curve order of the nodes, each tile's stencil-column union staged by asynchronous
-   copies) and in difference form, sum_t w_t (v_t - v_i) + (sum_t w_t) v_i, whose FP32 error
-   scales with the field's differences rather than its size. */
+   copies, groups of 8 rows applied together with dense weights over the group's columns)
+   and in difference form, sum_t w_t (v_t - v_ref) + (sum_t w_t) v_ref with v_ref a node of
+   the tile, whose FP32 error scales with the field's differences rather than its size. */
 int rbffd_rk4_create(rbffd_handle *h, rbffd_opset *const *sets, int nsets, const double *coef,
                      const uint8_t *fixed_rows, int nfields, int dtype, rbffd_rk4 **out);
 /* Advance u (device, in place) by nsteps steps of size dt.  Pairs of steps run as one
