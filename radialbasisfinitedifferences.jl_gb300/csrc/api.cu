@@ -123,6 +123,11 @@ static_assert(NBIN <= rbffd_handle::kClassStreams, "one class stream per shape c
 
 // Shape classes of one build run on forked streams (1) or one after another on the handle's
 // stream (0).
+// Chunks of rows of the drop-in calls' weight solves, whose CSC values are downloaded while
+// the later chunks solve (0: gather and download all values after the solves).
+#ifndef RBFFD_EXPORT_CHUNKS
+#define RBFFD_EXPORT_CHUNKS 8
+#endif
 #ifndef RBFFD_CLASS_CONCURRENT
 #define RBFFD_CLASS_CONCURRENT 1
 #endif
@@ -561,6 +566,14 @@ RBFFD_EXPORT int rbffd_synchronize(rbffd_handle *h)
 struct PatternHook {
     virtual int build(rbffd_handle *h, int64_t N, int n, const int64_t *row_ptr, const int32_t *nbr) = 0;
     virtual int download(rbffd_handle *h) = 0;
+    // > 0: the values are written straight into CSC order (csc_pos) and the systems are solved
+    // in that many chunks of consecutive rows; chunk_done(i) runs once chunk i's launch is on
+    // stream st (it may download the columns that chunks 0..i complete).
+    virtual int chunks() const { return 0; }
+    virtual const int32_t *csc_pos() const { return nullptr; }
+    virtual int chunk_done(rbffd_handle *, int, cudaStream_t, const double *, int64_t) { return RBFFD_OK; }
+    // After the FP64 re-solve of stalled systems (n_fallback of them).
+    virtual void solved(int64_t) {}
     virtual ~PatternHook() {}
 };
 
@@ -743,6 +756,11 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         int rc2 = hook->build(h, N, pb->n, row_ptr, nbr);
         if (rc2) return bail(rc2);
     }
+    const int nchunk = hook_on ? hook->chunks() : 0;
+    if (nchunk > 0) {  // the pattern's download first on the side stream, the values' behind it
+        int rc2 = hook->download(h);
+        if (rc2) return bail(rc2);
+    }
     int32_t *col;
     double *val;
     CK(keep.get(&col, nnz));
@@ -774,6 +792,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     a.max_refine = h->opt.max_refine;
     a.refine_tol = h->opt.refine_tol;
     a.unscaled_overload = unscaled;
+    if (nchunk > 0) a.csc_pos = hook->csc_pos();
     int32_t *fb_list = nullptr;
     if (pb->precision == RBFFD_PREC_MIXED) {
         CK(tmp.get(&fb_list, nsys));
@@ -814,9 +833,18 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
             ab.max_s = ab.max_n + ab.max_m;
             launches.push_back(ab);
         }
+    } else if (nchunk > 1 && nsys >= (int64_t)nchunk * 1024) {
+        // chunks of consecutive systems (rows), each its own persistent launch
+        for (int c = 0; c < nchunk; c++) {
+            SolveArgs ac = a;
+            ac.sys_base = (int64_t)c * nsys / nchunk;
+            ac.nsys = (int64_t)(c + 1) * nsys / nchunk - ac.sys_base;
+            launches.push_back(ac);
+        }
     } else {
         launches.push_back(a);
     }
+    const bool chunked = nchunk > 0 && (int)launches.size() == nchunk;
     {
         unsigned long long *claim;
         int32_t *sample_list;
@@ -827,9 +855,30 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         for (size_t i = 0; i < launches.size(); i++)
             CK(h->tuner.choose(launches[i], table, pb->precision, h->opt.warps_per_block, h->num_sms, sample_list, st,
                                &cfg[i]));
-        if (launches.size() == 1 || !RBFFD_CLASS_CONCURRENT) {
+        if (chunked) {
+            // chunks alternate between two forked streams, so that a chunk's persistent CTAs
+            // start as the previous chunk's drain; the columns each chunk completes are
+            // downloaded on the side stream meanwhile (in chunk order there, so a download
+            // also follows every earlier chunk)
+            CK(cudaEventRecord(h->cls_ev[rbffd_handle::kClassStreams], st));
+            for (int k = 0; k < 2; k++) CK(cudaStreamWaitEvent(h->cls_st[k], h->cls_ev[rbffd_handle::kClassStreams], 0));
+            for (size_t i = 0; i < launches.size(); i++) {
+                cudaStream_t cs = h->cls_st[i & 1];
+                CK(launch_solve_config(launches[i], table, cfg[i], h->num_sms, cs));
+                int rc2 = hook->chunk_done(h, (int)i, cs, val, nnz);
+                if (rc2) return bail(rc2);
+            }
+            for (int k = 0; k < 2; k++) {
+                CK(cudaEventRecord(h->cls_ev[k], h->cls_st[k]));
+                CK(cudaStreamWaitEvent(st, h->cls_ev[k], 0));
+            }
+        } else if (launches.size() == 1 || !RBFFD_CLASS_CONCURRENT) {
             for (size_t i = 0; i < launches.size(); i++)
                 CK(launch_solve_config(launches[i], table, cfg[i], h->num_sms, st));
+            for (int c = 0; c < nchunk; c++) {  // values in CSC order but solved in one launch
+                int rc2 = hook->chunk_done(h, c, st, val, nnz);
+                if (rc2) return bail(rc2);
+            }
         } else {
             CK(cudaEventRecord(h->cls_ev[rbffd_handle::kClassStreams], st));
             for (size_t i = 0; i < launches.size(); i++) {
@@ -843,7 +892,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         n_solve_launches = (int64_t)launches.size();
         h->tune_report = h->tuner.report();
     }
-    if (hook_on) {
+    if (hook_on && nchunk == 0) {
         int rc2 = hook->download(h);
         if (rc2) return bail(rc2);
     }
@@ -856,6 +905,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         CK(launch_solve_fp64_subset(a, table, wpb, h->num_sms, st, hf.fallback_count));
         CK(cudaMemcpyAsync(&hf.first_bad, &dflags->first_bad, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     }
+    if (hook_on) hook->solved(pb->precision == RBFFD_PREC_MIXED ? hf.fallback_count : 0);
     CK(cudaEventRecord(h->ev[5], st));
     CK(cudaStreamSynchronize(st));
     if (hf.knn_err) return bail(fail(h, RBFFD_EINVAL, "fewer candidate nodes than the stencil size"));
@@ -1634,12 +1684,27 @@ static int export_all(rbffd_handle *h, rbffd_opset *s, rbffd_csc *out)
 // The CSC pattern of a collocated uniform set depends on the stencils only, so the drop-in
 // calls build it before the weight solves and download colptr/rowval into every output on the
 // side stream while the solves run; the values follow once the solves finish.
+//
+// With nchunk > 0 the weight solves write their values straight into CSC order (csc_pos, the
+// inverse of the CSC gather permutation) and run in nchunk launches of consecutive rows; as
+// each completes, the CSC columns that no later row references are final and are downloaded
+// on the side stream while the next chunks solve, instead of gathering and downloading all
+// values after the solves.  Systems that the FP64 fallback re-solves afterwards make the
+// export download every value again.
 struct EarlyCsc : PatternHook {
     rbffd_csc *out = nullptr;
     int nops = 0;
     int64_t N = 0, nnz = 0;
     int64_t *colstart = nullptr, *rowval = nullptr, *perm = nullptr;
     bool active = false;
+    int nchunk = 0;                 // requested; 0 after build() when chunking does not apply
+    int32_t *inv = nullptr;         // CSR position -> CSC position
+    int64_t hcp[RBFFD_MAX_CHUNKS] = {};  // CSC entries final after chunks 0..i
+    cudaEvent_t chunk_ev[RBFFD_MAX_CHUNKS] = {};
+    int64_t n_fallback = 0;
+
+    int chunks() const override { return active ? nchunk : 0; }
+    const int32_t *csc_pos() const override { return inv; }
 
     int build(rbffd_handle *h, int64_t N_, int n, const int64_t *row_ptr, const int32_t *nbr) override
     {
@@ -1670,8 +1735,41 @@ struct EarlyCsc : PatternHook {
         CK(cudaFreeAsync(fill, st));
         CK(cudaFreeAsync(scratch, st));
         CK(cudaEventRecord(h->side_ev[0], st));
+        if (nchunk > 0 && (nchunk > RBFFD_MAX_CHUNKS || nnz > INT32_MAX || N < (int64_t)nchunk * 1024)) nchunk = 0;
+        if (nchunk > 0) {
+            int *cm;
+            int64_t *cp;
+            CK(cudaMallocAsync((void **)&inv, sizeof(int32_t) * nnz, st));
+            CK(cudaMallocAsync((void **)&cm, sizeof(int) * nchunk, st));
+            CK(cudaMallocAsync((void **)&cp, sizeof(int64_t) * nchunk, st));
+            CK(launch_invert_perm(nnz, perm, inv, st));
+            CK(launch_chunk_bounds(N, n, nbr, nchunk, colstart, cm, cp, st));
+            CK(cudaMemcpyAsync(hcp, cp, sizeof(int64_t) * nchunk, cudaMemcpyDeviceToHost, st));
+            CK(cudaFreeAsync(cm, st));
+            CK(cudaFreeAsync(cp, st));
+            CK(cudaStreamSynchronize(st));
+            for (int i = 0; i < nchunk; i++)
+                if (!chunk_ev[i]) CK(cudaEventCreateWithFlags(&chunk_ev[i], cudaEventDisableTiming));
+        }
         return RBFFD_OK;
     }
+
+    // Columns final after chunk i: CSC entries [hcp[i-1], hcp[i]) of every operator.
+    int chunk_done(rbffd_handle *h, int i, cudaStream_t cs, const double *val, int64_t nnz_) override
+    {
+        cudaStream_t ss = h->side;
+        CK(cudaEventRecord(chunk_ev[i], cs));
+        CK(cudaStreamWaitEvent(ss, chunk_ev[i], 0));
+        const int64_t a = i ? hcp[i - 1] : 0, b = hcp[i];
+        if (b <= a) return RBFFD_OK;
+        for (int q = 0; q < nops; q++)
+            if (out[q].nzval)
+                CK(cudaMemcpyAsync(out[q].nzval + a, val + (size_t)q * nnz_ + a, sizeof(double) * (b - a),
+                                   cudaMemcpyDeviceToHost, ss));
+        return RBFFD_OK;
+    }
+
+    void solved(int64_t nfb) override { n_fallback = nfb; }
 
     int download(rbffd_handle *h) override
     {
@@ -1693,8 +1791,15 @@ struct EarlyCsc : PatternHook {
         if (colstart) cudaFreeAsync(colstart, h->side);
         if (rowval) cudaFreeAsync(rowval, h->side);
         if (perm) cudaFreeAsync(perm, h->side);
+        if (inv) cudaFreeAsync(inv, h->side);
         cudaStreamSynchronize(h->side);
         colstart = rowval = perm = nullptr;
+        inv = nullptr;
+        for (cudaEvent_t &e : chunk_ev)
+            if (e) {
+                cudaEventDestroy(e);
+                e = nullptr;
+            }
     }
 };
 
@@ -1706,12 +1811,27 @@ static int build_and_export(rbffd_handle *h, const rbffd_problem *pb, int unscal
     EarlyCsc ec;
     ec.out = out;
     ec.nops = __builtin_popcount(pb->op_mask);
+    ec.nchunk = RBFFD_EXPORT_CHUNKS;
     int rc = opset_build(h, pb, unscaled, &s, stats, &ec);
     if (rc) {
         ec.release(h);
         return rc;
     }
-    if (ec.active) {
+    if (ec.active && ec.nchunk > 0) {
+        // the values were written in CSC order and downloaded chunk by chunk; systems re-solved
+        // by the FP64 fallback after their chunk's download need the values again
+        cudaError_t e = cudaSuccess;
+        if (ec.n_fallback > 0) {
+            e = cudaStreamWaitEvent(h->side, h->ev[5], 0);
+            for (int q = 0; q < s->nops && e == cudaSuccess; q++)
+                if (out[q].nzval)
+                    e = cudaMemcpyAsync(out[q].nzval, s->val + (size_t)q * s->nnz, sizeof(double) * s->nnz,
+                                        cudaMemcpyDeviceToHost, h->side);
+        }
+        cudaError_t e2 = cudaStreamSynchronize(h->side);
+        if (e == cudaSuccess) e = e2;
+        rc = e == cudaSuccess ? RBFFD_OK : fail(h, RBFFD_ECUDA, std::string("csc export: ") + cudaGetErrorString(e));
+    } else if (ec.active) {
         // values in CSC order: each operator gathered into its own buffer on the main stream and
         // downloaded on the side stream as soon as its gather is done, so that the copies of
         // one operator overlap the gathers of the next

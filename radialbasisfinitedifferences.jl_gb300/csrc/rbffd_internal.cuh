@@ -156,7 +156,9 @@ struct SolveArgs {
     const int32_t *deg_node;   // nullable per-node degree
     int n, deg;                // uniform values
     const int32_t *sys_node;   // X node of every system
-    const int32_t *sys_list;   // nullable: this launch solves systems sys_list[0..nsys), else 0..nsys
+    const int32_t *sys_list;   // nullable: this launch solves systems sys_list[0..nsys), else
+                               // sys_base + 0..nsys
+    int64_t sys_base;
     const int64_t *sys_rows;   // nullable: rows of system i are rows_list[sys_rows[i]..sys_rows[i+1])
     const int32_t *rows_list;  // row ids (global evaluation-point ids)
     int64_t nsys;
@@ -175,6 +177,8 @@ struct SolveArgs {
     int unscaled_overload;     // generate_operator(X,p,n,polydeg) quirk
     unsigned long long *next_sys;  // nullable, zeroed: the solve kernels claim systems from this
                                    // counter instead of a fixed grid stride
+    const int32_t *csc_pos;        // nullable: entry e of the CSR layout is stored at val position
+                                   // csc_pos[e] (the CSC order of an export), col stays CSR
 };
 
 cudaError_t launch_solve_fp64(const SolveArgs &a, const OpTable &ops, int warps_per_block,
@@ -243,4 +247,13 @@ cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int
 cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *src, double *dst,
                               cudaStream_t st);
 cudaError_t launch_add_i64(int64_t n, int64_t *a, int64_t v, cudaStream_t st);
+// inv[perm[k]] = k (the CSR -> CSC position map of an export).
+cudaError_t launch_invert_perm(int64_t nnz, const int64_t *perm, int32_t *inv, cudaStream_t st);
+// Collocated uniform stencils (row r = node r, nbr N x n) solved in C chunks of consecutive
+// rows: cp[i] = the number of leading CSC entries (columns referenced only by rows of chunks
+// <= i) that are final once chunks 0..i are solved; colstart1 = the 1-based CSC column starts;
+// cm: C ints of scratch.
+constexpr int RBFFD_MAX_CHUNKS = 8;
+cudaError_t launch_chunk_bounds(int64_t N, int n, const int32_t *nbr, int C, const int64_t *colstart1, int *cm,
+                                int64_t *cp, cudaStream_t st);
 cudaError_t launch_f64_to_f32(int64_t n, const double *a, float *b, cudaStream_t st);

@@ -832,8 +832,11 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
                                                 double yy, const double *sc, bool need_rinv, double *B, int lane)
 {
     const int r = ops.nops;
+    const bool at0 = is_zero64(yx) && is_zero64(yy);
     for (int i = lane; i < n; i += 32) {
-        double cx = yx - xs[2 * i], cy = yy - xs[2 * i + 1];
+        // y~ - x~_i; at the centre (the collocated case) the negation is a sign flip on the
+        // integer pipe instead of an FP64 subtraction from zero
+        double cx = at0 ? neg64(xs[2 * i]) : yx - xs[2 * i], cy = at0 ? neg64(xs[2 * i + 1]) : yy - xs[2 * i + 1];
         if (is_zero64(cx)) cx = EPS64;
         if (is_zero64(cy)) cy = EPS64;
         const double r2 = fma(cx, cx, cy * cy);
@@ -855,15 +858,14 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
                         for (int e = 0; e < tm.er; e++) tv *= rr;
                     else
                         for (int e = 0; e < -tm.er; e++) tv *= rinv;
-                    cv += tv;
+                    cv = t == 0 ? tv : cv + tv;  // no FP64 addition to an initial zero
                 }
                 if (od.ncomp > 1) cv *= sc[2 * q + cidx];
-                v += cv;
+                v = cidx == 0 ? cv : v + cv;
             }
             B[i * r + q] = v;
         }
     }
-    const bool at0 = is_zero64(yx) && is_zero64(yy);
     for (int l = lane; l < m; l += 32) {
         int t = 0, rem = l;
         while (rem > t) {
@@ -902,14 +904,12 @@ __device__ __forceinline__ void write_row_df(const SolveArgs &a, const OpTable &
     const int64_t off = a.row_ptr[row - a.row_begin];
     const int r = ops.nops;
     for (int l = lane; l < n; l += 32) a.col[off + l] = sid[l];
-    for (int q = 0; q < r; q++) {
-        double *dst = a.val + (int64_t)q * a.nnz + off;
-        const bool ps = ops.op[q].post_scale;
-        const double f = sc[2 * q];
-        for (int l = lane; l < n; l += 32) {
+    for (int l = lane; l < n; l += 32) {
+        const int64_t d = a.csc_pos ? (int64_t)a.csc_pos[off + l] : off + l;
+        for (int q = 0; q < r; q++) {
             const float2 x = X2[l * r + q];
             const double v = f32_to_f64(x.x) + f32_to_f64(x.y);
-            dst[l] = ps ? f * v : v;
+            a.val[(int64_t)q * a.nnz + d] = ops.op[q].post_scale ? sc[2 * q] * v : v;
         }
     }
 }
@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
             ts += nw;
             if (ts >= a.nsys) break;
         }
-        const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
+        const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : a.sys_base + ts;
         const int j = a.sys_node[sys];
         const int n = a.n_node ? a.n_node[j] : a.n;
         const int deg = a.deg_node ? a.deg_node[j] : a.deg;

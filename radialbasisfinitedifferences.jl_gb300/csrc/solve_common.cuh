@@ -90,6 +90,11 @@ __device__ __forceinline__ float warp_max_f(float v)
 }
 
 __device__ __forceinline__ bool is_zero64(double x) { return abs_key(x) == 0ull; }
+// -x by flipping the sign bit (integer pipe; exact, like the FP64 negation)
+__device__ __forceinline__ double neg64(double x)
+{
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
 
 // sqrt(a) for a positive normal double, without a library call: an FP32 reciprocal square
 // root of the mantissa (exponent split off on the integer pipe, a = a' 4^k with a' in [1, 4))
@@ -569,8 +574,9 @@ __device__ __forceinline__ void build_rhs(const OpTable &ops, const double *xs, 
             cx = xs[2 * i];
             cy = xs[2 * i + 1];
         } else {
-            cx = yx - xs[2 * i];
-            cy = yy - xs[2 * i + 1];
+            const bool at0 = is_zero64(yx) && is_zero64(yy);  // the collocated case: a sign flip
+            cx = at0 ? neg64(xs[2 * i]) : yx - xs[2 * i];
+            cy = at0 ? neg64(xs[2 * i + 1]) : yy - xs[2 * i + 1];
             if (is_zero64(cx)) cx = EPS64;
             if (is_zero64(cy)) cy = EPS64;
         }
@@ -600,10 +606,10 @@ __device__ __forceinline__ void build_rhs(const OpTable &ops, const double *xs, 
                         for (int e = 0; e < tm.er; e++) tv *= rr;
                     else
                         for (int e = 0; e < -tm.er; e++) tv *= rinv;
-                    cv += tv;
+                    cv = t == 0 ? tv : cv + tv;  // no FP64 addition to an initial zero
                 }
                 if (od.ncomp > 1) cv *= ipow(sx, oc.a) * ipow(sy, oc.b);
-                v += cv;
+                v = cidx == 0 ? cv : v + cv;
             }
             B[row * r + q] = v;
         }
@@ -642,12 +648,11 @@ __device__ __forceinline__ void write_row(const SolveArgs &a, const OpTable &ops
     for (int l = lane; l < n; l += 32) a.col[off + l] = sid[l];
     for (int q = 0; q < r; q++) {
         const OpDesc &od = ops.op[q];
-        double *dst = a.val + (int64_t)q * a.nnz + off;
-        if (od.post_scale) {
-            double f = ipow(sx, od.c[0].a) * ipow(sy, od.c[0].b);
-            for (int l = lane; l < n; l += 32) dst[l] = f * Xs[l * r + q];
-        } else {
-            for (int l = lane; l < n; l += 32) dst[l] = Xs[l * r + q];
+        double *dst = a.val + (int64_t)q * a.nnz;
+        const double f = od.post_scale ? ipow(sx, od.c[0].a) * ipow(sy, od.c[0].b) : 1.0;
+        for (int l = lane; l < n; l += 32) {
+            const int64_t d = a.csc_pos ? (int64_t)a.csc_pos[off + l] : off + l;
+            dst[d] = od.post_scale ? f * Xs[l * r + q] : Xs[l * r + q];
         }
     }
 }

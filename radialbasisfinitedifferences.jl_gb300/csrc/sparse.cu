@@ -803,6 +803,46 @@ __global__ void gather_f64_kernel(int64_t n, const int64_t *perm, const double *
         dst[t] = src[perm[t]];
 }
 
+__global__ void invert_perm_kernel(int64_t n, const int64_t *perm, int32_t *inv)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x)
+        inv[perm[t]] = (int32_t)t;
+}
+
+// cm[k] = min over the rows of chunk k (rows [k N / C, (k + 1) N / C)) of the smallest column
+// the row's stencil references; per-block minima first, one atomic per block and chunk.
+__global__ void chunk_min_col_kernel(int64_t N, int n, const int32_t *nbr, int C, int *cm)
+{
+    __shared__ int bm[RBFFD_MAX_CHUNKS];
+    for (int k = threadIdx.x; k < C; k += blockDim.x) bm[k] = INT_MAX;
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+        int mc = INT_MAX;
+        for (int t = 0; t < n; t++) mc = min(mc, nbr[r * n + t]);
+        int k = 0;
+        while (k + 1 < C && r >= (int64_t)(k + 1) * N / C) k++;
+        atomicMin(&bm[k], mc);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < C; k += blockDim.x)
+        if (bm[k] != INT_MAX) atomicMin(&cm[k], bm[k]);
+}
+
+// Columns [0, cb[i]) are referenced only by rows of chunks <= i: cb[i] = min over k > i of
+// cm[k] (all columns after the last chunk); cp[i] = their CSC entry count (colstart 1-based).
+__global__ void chunk_bounds_kernel(int64_t N, int C, const int *cm, const int64_t *colstart1, int64_t *cp)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t b = N;
+    for (int i = C - 1; i >= 0; i--) {
+        cp[i] = colstart1[b] - 1;
+        if (i > 0 && (int64_t)cm[i] < b) b = cm[i];
+    }
+    for (int i = 1; i < C; i++)  // monotone (each bound covers the one before)
+        if (cp[i] < cp[i - 1]) cp[i] = cp[i - 1];
+}
+
 __global__ void add_i64_kernel(int64_t n, int64_t *a, int64_t v)
 {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
@@ -1049,6 +1089,23 @@ cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *sr
                               cudaStream_t st)
 {
     gather_f64_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, perm, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_invert_perm(int64_t nnz, const int64_t *perm, int32_t *inv, cudaStream_t st)
+{
+    invert_perm_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, perm, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chunk_bounds(int64_t N, int n, const int32_t *nbr, int C, const int64_t *colstart1, int *cm,
+                                int64_t *cp, cudaStream_t st)
+{
+    if (C < 1 || C > RBFFD_MAX_CHUNKS) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(cm, 0x7f, sizeof(int) * C, st);  // 0x7f7f7f7f: above any column
+    if (e != cudaSuccess) return e;
+    chunk_min_col_kernel<<<blocks_for(N, 256, 4096), 256, 0, st>>>(N, n, nbr, C, cm);
+    chunk_bounds_kernel<<<1, 32, 0, st>>>(N, C, cm, colstart1, cp);
     return cudaGetLastError();
 }
 

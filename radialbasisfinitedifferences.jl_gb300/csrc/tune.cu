@@ -78,13 +78,13 @@ SolveConfig heuristic(const SolveArgs &a, const OpTable &t, int precision, int f
 }
 
 // out[i] = the class's system at position floor(i * nsys / sample) (list[...] when the class is a
-// list of systems, the position itself otherwise).
-__global__ void sample_list_kernel(const int32_t *list, int64_t nsys, int64_t sample, int32_t *out)
+// list of systems, base + the position otherwise).
+__global__ void sample_list_kernel(const int32_t *list, int64_t base, int64_t nsys, int64_t sample, int32_t *out)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= sample) return;
     const int64_t pos = i * nsys / sample;
-    out[i] = list ? list[pos] : (int32_t)pos;
+    out[i] = list ? list[pos] : (int32_t)(base + pos);
 }
 
 const char *kernel_name(int k)
@@ -117,13 +117,14 @@ cudaError_t SolveTuner::choose(const SolveArgs &a, const OpTable &t, int precisi
     // enough systems to fill every SM a few times over
     const int64_t sample = tune_sample_systems(num_sms);
     std::vector<SolveConfig> cand = candidates(a, t, precision);
-    if (fixed_wpb > 0 || a.nsys < 3 * sample || a.nsys > INT32_MAX || cand.size() < 2 || !a.next_sys ||
+    if (fixed_wpb > 0 || a.nsys < 3 * sample || a.sys_base + a.nsys > INT32_MAX || cand.size() < 2 || !a.next_sys ||
         !sample_list) {
         // a small class is not cached: a later, larger class of the same shape may be timed
         *out = heuristic(a, t, precision, fixed_wpb);
         return cudaSuccess;
     }
-    sample_list_kernel<<<(unsigned)((sample + 255) / 256), 256, 0, st>>>(a.sys_list, a.nsys, sample, sample_list);
+    sample_list_kernel<<<(unsigned)((sample + 255) / 256), 256, 0, st>>>(a.sys_list, a.sys_base, a.nsys, sample,
+                                                                         sample_list);
     cudaError_t lerr = cudaGetLastError();
     if (lerr != cudaSuccess) return lerr;
     cudaEvent_t e0, e1;

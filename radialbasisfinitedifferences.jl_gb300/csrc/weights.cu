@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) solve_fp64_kernel(SolveArgs a, OpTable op
         return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
     };
     for (int64_t w = claim ? next(0) : gw; w < nwork; w = next(w)) {
-        int64_t sys = subset ? (int64_t)subset[w] : (a.sys_list ? (int64_t)a.sys_list[w] : w);
+        int64_t sys = subset ? (int64_t)subset[w] : (a.sys_list ? (int64_t)a.sys_list[w] : a.sys_base + w);
         int j = a.sys_node[sys];
         int n = a.n_node ? a.n_node[j] : a.n;
         int deg = a.deg_node ? a.deg_node[j] : a.deg;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) solve_mixed_kernel(SolveArgs a, OpTable o
         return (int64_t)__shfl_sync(RBFFD_FULL, v, 0);
     };
     for (int64_t ts = a.next_sys ? next(0) : gw; ts < a.nsys; ts = next(ts)) {
-        const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : ts;
+        const int64_t sys = a.sys_list ? (int64_t)a.sys_list[ts] : a.sys_base + ts;
         int j = a.sys_node[sys];
         int n = a.n_node ? a.n_node[j] : a.n;
         int deg = a.deg_node ? a.deg_node[j] : a.deg;

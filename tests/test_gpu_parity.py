@@ -150,6 +150,31 @@ def test_generate_operator_collocated_csc(pkg, orc, gpu, n):
         assert np.abs(A.data - nz).max() <= FP64_TOL * scale * 10
 
 
+@pytest.mark.parametrize("precision,max_refine", [("mixed", 0), ("fp64", 0), ("mixed", 1)])
+def test_generate_operator_chunked_export(pkg, orc, gpu, precision, max_refine):
+    """Collocated drop-in calls of >= 8192 nodes write the values in CSC order and download
+    them in 8 row chunks while later chunks solve.  The CSC equals sparse(I, J, V) of the
+    oracle in both precisions, and when every mixed system falls back to FP64 after its
+    chunk's download (max_refine = 1) the values are downloaded again."""
+    import scipy.sparse as sp
+
+    X, _ = grid(pkg, 100, seed=6)
+    N, p, n, deg = len(X), 3, 30, 3
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    with pkg.Handle(max_refine=max_refine) as h:
+        mats = pkg.generate_operator(X, X, p, n, deg, ops=ops, precision=precision, handle=h)
+    tol = FP64_TOL if precision == "fp64" or max_refine == 1 else MIXED_TOL
+    for q, A in enumerate(mats):
+        cp, rv, nz = orc.to_csc(N, N, ref["cols"], ref["W"][q])
+        assert np.array_equal(A.indptr, cp - 1)
+        assert np.array_equal(A.indices, rv - 1)
+        # row-relative error, rows of both in column order
+        got = A.tocsr().data.reshape(N, n)
+        want = sp.csc_matrix((nz, rv - 1, cp - 1), shape=(N, N)).tocsr().data.reshape(N, n)
+        assert rel_row_err(got, want) <= tol, q
+
+
 def test_unscaled_overload(pkg, orc, gpu):
     X, _ = grid(pkg, 32, seed=8)
     p, n, deg = 3, 15, 2
