@@ -1063,9 +1063,14 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
                 const float xmax = __uint_as_float(xkey);
                 const float e_cur = xmax > 0.0f ? __fdividef(dmax, xmax) : 0.0f;
                 if (!(e_cur == e_cur) || isinf(e_cur)) break;
+                // Predicted error after this correction: rho * e_cur, rho the observed contraction.
+                // rho is taken from two corrections (it >= 2): at it = 1 the ratio to the first
+                // solve measures the error of x0 in the direction of the solution only and can
+                // fall far below the contraction (systems stopped there erred ~1e3x the
+                // tolerance at refine_tol 1e-11).
                 if (it >= 1) {
                     const float rho = e_prev > 0.0f ? __fdividef(e_cur, e_prev) : 0.0f;
-                    if (rho * e_cur <= tol32 || e_cur == 0.0f) {
+                    if (e_cur == 0.0f || (it >= 2 && rho * e_cur <= tol32)) {
                         conv = true;
                         break;
                     }

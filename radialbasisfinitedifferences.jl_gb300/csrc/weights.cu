@@ -192,9 +192,9 @@ __global__ void __launch_bounds__(256) solve_mixed_kernel(SolveArgs a, OpTable o
                 __syncwarp();
                 float e_cur = xmax > 0.0f ? dmax / xmax : 0.0f;
                 if (!(e_cur == e_cur) || isinf(e_cur)) break;  // NaN / inf
-                if (it >= 1) {
+                if (it >= 1) {  // the contraction rho from two corrections, as in schur.cuh
                     float rho = e_prev > 0.0f ? e_cur / e_prev : 0.0f;
-                    if ((double)rho * (double)e_cur <= a.refine_tol || e_cur == 0.0f) {
+                    if (e_cur == 0.0f || (it >= 2 && (double)rho * (double)e_cur <= a.refine_tol)) {
                         conv = true;
                         break;
                     }

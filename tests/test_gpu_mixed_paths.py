@@ -187,3 +187,19 @@ def test_fixed_cta_size_beyond_shared_memory(pkg, orc, gpu, wpb, precision):
     with pkg.Handle(warps_per_block=wpb) as h:
         with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision=precision, handle=h) as s:
             check_against_oracle(s, ref, ops, n, HARD_TOL)
+
+
+@pytest.mark.parametrize("tol", [1e-11, 1e-10])
+def test_loose_refine_tol_keeps_its_promise(pkg, orc, gpu, tol):
+    """A looser refine_tol stops the refinement earlier, but only on a contraction measured
+    from two corrections: the weights stay within ~10 x the tolerance of the oracle (stopping
+    on the first correction's estimate erred by ~1e3 x the tolerance)."""
+    X = grid(pkg, 64, seed=23)
+    p, n, deg = 3, 30, 3
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, X, p, n, deg, ops)
+    with pkg.Handle(refine_tol=tol) as h:
+        with pkg.OperatorSet(X, None, p, n, deg, ops=ops, precision="mixed", handle=h) as s:
+            st = s.stats.as_dict()
+            assert st["refine_hist"][1] == 0, st
+            check_against_oracle(s, ref, ops, n, max(MIXED_TOL, 10 * tol))
