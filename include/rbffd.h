@@ -152,7 +152,10 @@ int rbffd_synchronize(rbffd_handle *h);
    node_class != NULL, the boundary-aware overload generate_operator(X, Y, p, n, polydeg,
    X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y_idx_bc, Y_idx_bc_g) -- :192-352.
    out[] has one rbffd_csc per set bit of op_mask, in increasing bit order; each is an
-   M x N matrix with nnz = M * n.  Y == X (same pointer, M == N) is the collocated case. */
+   M x N matrix with nnz = M * n.  Y == X (same pointer, M == N) is the collocated case.
+   Collocated calls with one stencil size download the CSC pattern while the weights are
+   solved and, from 8192 nodes on, the values of each completed range of columns while the
+   remaining rows solve; the outputs are complete when the call returns. */
 int rbffd_generate_operator(rbffd_handle *h, const double *X, int64_t N, const double *Y,
                             int64_t M, int p, int n, int polydeg, const int32_t *node_class,
                             uint32_t op_mask, int precision, rbffd_csc *out,

@@ -163,6 +163,14 @@ cudaError_t SolveTuner::choose(const SolveArgs &a, const OpTable &t, int precisi
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return err;
+    // Among Schur configurations within 1.5 % of the fastest, the widest CTA: its warps start
+    // their systems together, which keeps them in the same part of the kernel over a long
+    // launch, an advantage a short sample does not show (1,048,576 30-node systems: 8 warps
+    // per CTA 42.9 ms, 4 warps 43.4 ms, tied at 0.420 ms on the sample).
+    if (win.kernel == SOLVE_KERNEL_SCHUR)
+        for (size_t i = 0; i < rec.cand.size(); i++)
+            if (rec.cand[i].kernel == SOLVE_KERNEL_SCHUR && rec.ms[i] <= best * 1.015f && rec.cand[i].wpb > win.wpb)
+                win = rec.cand[i];
     // the sample systems are solved again by the real launch: clear what they counted
     if (a.fallback_count && (err = cudaMemsetAsync(a.fallback_count, 0, sizeof(int), st)) != cudaSuccess) return err;
     if (a.hist && (err = cudaMemsetAsync(a.hist, 0, 8 * sizeof(unsigned long long), st)) != cudaSuccess) return err;
