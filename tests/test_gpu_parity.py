@@ -299,6 +299,30 @@ def test_boundary_aware_generate(pkg, orc, gpu):
         assert (np.abs(W - Wr).max(1) / np.abs(Wr).max(1)).max() < FP64_TOL, ALL6[q]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_boundary_aware_generate_chunked(pkg, orc, gpu, precision):
+    """The boundary-aware drop-in overload above 8192 nodes: the CSC values are written in
+    CSC order and downloaded by row chunks (boundary and ghost rows reference columns far
+    from their own index, which the chunk bounds must cover)."""
+    import scipy.sparse as sp
+
+    d = pkg.nodesets.rectangle_with_ghosts(total=10000, seed=13)
+    X, cls = d["X"], d["node_class"]
+    N = len(X)
+    ids = np.arange(1, N + 1)
+    rin, rbc, rg = ids[cls == 0], [ids[cls == b] for b in range(1, 5)], [ids[cls == -b] for b in range(1, 5)]
+    p, n, deg = 3, 20, 2
+    mats = pkg.generate_operator(X, X, p, n, deg, rin, rbc, rg, rin, rbc, rg, precision=precision)
+    ref = orc.generate(X, X, p, n, deg, ALL6, cls=cls)
+    for q, A in enumerate(mats):
+        cp, rv, nz = orc.to_csc(N, N, ref["cols"], ref["W"][q])
+        assert np.array_equal(A.indptr, cp - 1)
+        assert np.array_equal(A.indices, rv - 1)
+        got = A.tocsr().data.reshape(N, n)
+        want = sp.csc_matrix((nz, rv - 1, cp - 1), shape=(N, N)).tocsr().data.reshape(N, n)
+        assert rel_row_err(got, want) < tol_for(p, deg, precision), ALL6[q]
+
+
 def test_uneven_batch(pkg, orc, gpu):
     d = pkg.nodesets.rectangle_with_ghosts(total=8000, seed=12, main_fraction=0.5)
     X, cls, nn, dd = d["X"], d["node_class"], d["n"], d["deg"]
