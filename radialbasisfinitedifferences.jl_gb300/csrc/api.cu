@@ -123,6 +123,13 @@ static_assert(NBIN <= rbffd_handle::kClassStreams, "one class stream per shape c
 
 // Shape classes of one build run on forked streams (1) or one after another on the handle's
 // stream (0).
+// Mean nodes per cell of the kNN grid.  Measured at 1M nodes, k = 30 (kNN ms): 0.5 nodes per
+// cell 2.95, 0.75 2.73, 1 2.50, 1.25 3.59, 1.5 2.58, 2 2.99, 3 2.67, 4 2.62; the uneven batch
+// (k 20..60, boundary classes) 4.50 at 1 against 5.05 at 2.  The first search square (knn_r0)
+// follows from it.
+#ifndef RBFFD_GRID_NODES_PER_CELL
+#define RBFFD_GRID_NODES_PER_CELL 1.0
+#endif
 // Chunks of rows of the drop-in calls' weight solves, whose CSC values are downloaded while
 // the later chunks solve (0: gather and download all values after the solves).
 #ifndef RBFFD_EXPORT_CHUNKS
@@ -331,7 +338,7 @@ int build_grid(rbffd_handle *h, Arena &ar, const double2 *dX, const int32_t *dcl
     if (hbad) return fail(h, RBFFD_EINVAL, "non-finite node coordinates");
     double w = hb[1] - hb[0], hh = hb[3] - hb[2];
     double area = (w > 0 ? w : 1.0) * (hh > 0 ? hh : 1.0);
-    double cs = sqrt(2.0 * area / (double)N);
+    double cs = sqrt(RBFFD_GRID_NODES_PER_CELL * area / (double)N);
     if (!(cs > 0)) cs = 1.0;
     int64_t nx = (int64_t)(w / cs) + 1, ny = (int64_t)(hh / cs) + 1;
     while (nx * ny > 4 * N + 16) {
