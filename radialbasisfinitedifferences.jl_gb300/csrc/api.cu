@@ -145,19 +145,48 @@ __host__ __device__ inline int solve_bin(int n, int m)
 }
 
 // Per-bin system counts and largest n, m (cnt[0..NBIN), maxn[NBIN..2NBIN), maxm[2NBIN..3NBIN)).
+// Per class b: cnt[b] systems, cnt[NBIN + b] their largest n, cnt[2 NBIN + b] their largest m.
+// Warp-aggregated into shared memory (a ballot per class), then one global atomic per class
+// and block: three global atomics per system on 15 addresses took ~0.9 ms per 524,288 systems.
 __global__ void bin_count(const int32_t *sys_node, int64_t nsys, const int32_t *n_node, const int32_t *deg_node,
                           int n0, int deg0, unsigned long long *cnt)
 {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nsys;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int j = sys_node[t];
-        const int n = n_node ? n_node[j] : n0;
-        const int d = deg_node ? deg_node[j] : deg0;
-        const int m = (d + 1) * (d + 2) / 2;
-        const int b = solve_bin(n, m);
-        atomicAdd(cnt + b, 1ull);
-        atomicMax(cnt + NBIN + b, (unsigned long long)n);
-        atomicMax(cnt + 2 * NBIN + b, (unsigned long long)m);
+    __shared__ unsigned long long sc[3 * NBIN];
+    for (int i = threadIdx.x; i < 3 * NBIN; i += blockDim.x) sc[i] = 0ull;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nsys; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        const bool act = t < nsys;
+        int b = -1, n = 0, m = 0;
+        if (act) {
+            const int j = sys_node[t];
+            n = n_node ? n_node[j] : n0;
+            const int d = deg_node ? deg_node[j] : deg0;
+            m = (d + 1) * (d + 2) / 2;
+            b = solve_bin(n, m);
+        }
+#pragma unroll
+        for (int c = 0; c < NBIN; c++) {
+            const unsigned mask = __ballot_sync(RBFFD_FULL, b == c);
+            if (!mask) continue;
+            const unsigned mn = __reduce_max_sync(RBFFD_FULL, b == c ? (unsigned)n : 0u);
+            const unsigned mm = __reduce_max_sync(RBFFD_FULL, b == c ? (unsigned)m : 0u);
+            if (lane == 0) {
+                atomicAdd(&sc[c], (unsigned long long)__popc(mask));
+                atomicMax(&sc[NBIN + c], (unsigned long long)mn);
+                atomicMax(&sc[2 * NBIN + c], (unsigned long long)mm);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * NBIN; i += blockDim.x) {
+        if (i < NBIN) {
+            if (sc[i]) atomicAdd(cnt + i, sc[i]);
+        } else if (sc[i]) {
+            atomicMax(cnt + i, sc[i]);
+        }
     }
 }
 
@@ -165,17 +194,32 @@ struct BinOffsets {
     int64_t off[NBIN];
 };
 
+// The systems of class b listed from list[off[b]] on (in no particular order); one atomic per
+// class and warp.
 __global__ void bin_scatter(const int32_t *sys_node, int64_t nsys, const int32_t *n_node, const int32_t *deg_node,
                             int n0, int deg0, BinOffsets bo, unsigned long long *fill, int32_t *list)
 {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nsys;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int j = sys_node[t];
-        const int n = n_node ? n_node[j] : n0;
-        const int d = deg_node ? deg_node[j] : deg0;
-        const int b = solve_bin(n, (d + 1) * (d + 2) / 2);
-        const unsigned long long pos = atomicAdd(fill + b, 1ull);
-        list[bo.off[b] + (int64_t)pos] = (int32_t)t;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nsys; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        int b = -1;
+        if (t < nsys) {
+            const int j = sys_node[t];
+            const int n = n_node ? n_node[j] : n0;
+            const int d = deg_node ? deg_node[j] : deg0;
+            b = solve_bin(n, (d + 1) * (d + 2) / 2);
+        }
+#pragma unroll
+        for (int c = 0; c < NBIN; c++) {
+            const unsigned mask = __ballot_sync(RBFFD_FULL, b == c);
+            if (!mask) continue;
+            unsigned long long p0 = 0ull;
+            if (lane == __ffs(mask) - 1) p0 = atomicAdd(fill + c, (unsigned long long)__popc(mask));
+            p0 = __shfl_sync(RBFFD_FULL, p0, __ffs(mask) - 1);
+            if (b == c) list[bo.off[c] + (int64_t)p0 + __popc(mask & below)] = (int32_t)t;
+        }
     }
 }
 
@@ -823,7 +867,8 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
         int32_t *list;
         CK(tmp.zeros(&cnt, 4 * NBIN));
         CK(tmp.get(&list, nsys));
-        bin_count<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, cnt);
+        const int bblk = std::min(nblk(nsys), h->num_sms * 8);
+        bin_count<<<bblk, 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, cnt);
         CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         BinOffsets bo;
@@ -832,7 +877,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
             bo.off[b] = o;
             o += (int64_t)hc[b];
         }
-        bin_scatter<<<nblk(nsys), 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, bo,
+        bin_scatter<<<bblk, 256, 0, st>>>(sys_node, nsys, dn, ddeg, pb->n, pb->polydeg, bo,
                                                 cnt + 3 * NBIN, list);
         n_bin_launches = 2;
         for (int b = 0; b < NBIN; b++) {
