@@ -373,8 +373,18 @@ struct TileMeta {
 // stored one tile earlier); load the next tile's ids and offsets into registers; wait,
 // barrier; store the next tile's ids and offsets (nothing reads them before the next
 // barrier); warp g computes group g from shared memory and writes its 8 rows; barrier.
+// Resident CTAs per SM requested (registers) and the unroll of the column loop.  Measured at
+// 2048^2 nodes, 64 fields (ms per step): 3 CTAs unrolled 1x 5.12, 2x 5.02, 4x 5.25; 2 CTAs
+// unrolled 2x 5.46.
+#ifndef RBFFD_TILE_MINB
+#define RBFFD_TILE_MINB 3
+#endif
+#ifndef RBFFD_TILE_UNROLL
+#define RBFFD_TILE_UNROLL 2
+#endif
+constexpr int kTileUnroll = RBFFD_TILE_UNROLL;
 template <int F>
-__global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : 3)) rk4_tile_stage_kernel(StageArgs s)
+__global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : RBFFD_TILE_MINB)) rk4_tile_stage_kernel(StageArgs s)
 {
     extern __shared__ __align__(128) unsigned char ts_smem[];
     constexpr int FPL = F >= 32 ? F / 32 : 1, Q4 = F / 4;
@@ -425,6 +435,7 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : 3)) rk4_tile_stage_
             const uint4 *sl4 = reinterpret_cast<const uint4 *>(gsl + c0);
             const float4 *w4 = reinterpret_cast<const float4 *>(gwt + (size_t)c0 * TG);
             const float *fbl = fb + lofs;
+#pragma unroll kTileUnroll
             for (int j = 0; j < cn; j += 4) {
                 const uint4 s4 = sl4[j >> 2];
                 const uint32_t sc[4] = {s4.x, s4.y, s4.z, s4.w};
