@@ -520,7 +520,12 @@ __device__ __forceinline__ void warp_sort32(unsigned long long &cd, int &ci, int
 
 // Candidates of one batch that enter the list; at least this many are merged in bulk (sort +
 // merge, ~250 instructions) rather than inserted one at a time (~25 each).
-constexpr int MERGE_MIN = 10;
+// Survivor batches of at least this many keys are merged in bulk (sort + ranks), smaller ones
+// inserted one by one.  1M nodes, k = 30: 2.50 / 2.50 / 2.47 ms at 6 / 10 / 14.
+#ifndef RBFFD_KNN_MERGE_MIN
+#define RBFFD_KNN_MERGE_MIN 10
+#endif
+constexpr int MERGE_MIN = RBFFD_KNN_MERGE_MIN;
 
 // Exact FP64 keys of the queued candidates queue[0..cnt) (one per lane) and their insertion.
 template <int KS>
@@ -624,8 +629,13 @@ __device__ __forceinline__ void sweep_segments(const GridDev &g, TopK<KS> &tk, i
     __syncwarp();
 }
 
+// Resident 256-thread CTAs per SM requested for k <= 32 (64 registers); 5 (51 registers):
+// 2.62 against 2.50 ms.
+#ifndef RBFFD_KNN_MINB
+#define RBFFD_KNN_MINB 4
+#endif
 template <int KS>
-__global__ void __launch_bounds__(256, (KS == 1 ? 4 : 2)) knn_kernel(GridDev g, const double2 *__restrict__ Q,
+__global__ void __launch_bounds__(256, (KS == 1 ? RBFFD_KNN_MINB : 2)) knn_kernel(GridDev g, const double2 *__restrict__ Q,
                                                   const int32_t *__restrict__ qcls,
                                                   const int32_t *__restrict__ q_node,
                                                   bool node_query, int64_t nq,

@@ -129,7 +129,7 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t 
 
 // mode 0: cnt[tile] = union size, gcnt[tile * 8 + g] = group g's column count rounded up to a
 // multiple of 4.  mode 1: union ids, group columns and weights, row records.
-__global__ void __launch_bounds__(256) tile_build_kernel(TileOp t, int64_t rows, const int32_t *__restrict__ order,
+__global__ void __launch_bounds__(32 * NGRP) tile_build_kernel(TileOp t, int64_t rows, const int32_t *__restrict__ order,
                                                          const int64_t *__restrict__ row_ptr,
                                                          const int32_t *__restrict__ col,
                                                          const float *__restrict__ val32,
