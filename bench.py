@@ -763,12 +763,18 @@ def rk4_results(args):
         res[dt_name] = (u, ms)
         sz = 8 if dt_name == "f64" else 4
         nnz = s3.nnz
-        # the stencil application of one stage: weights and column ids once, the fields read
-        # once and the stage result written once
-        stage_bytes = nnz * (sz + 4) + 2 * N * F * sz
-        gbps = 4 * args.rk_steps * stage_bytes / (ms * 1e-3) / 1e9
+        # one Horner stage out = u + c L v: the weights and column ids once, the stage input v
+        # and the state u read once each and the result written once; the first stage of a
+        # step has v = u (one array read), so a step moves 4 nnz (sz + 4) + 11 N F sz bytes
+        step_bytes = 4 * nnz * (sz + 4) + (2 + 3 * 3) * N * F * sz
+        stage_bytes = step_bytes / 4
+        gbps = args.rk_steps * step_bytes / (ms * 1e-3) / 1e9
         out[f"{dt_name}"] = {"ms_per_step": ms / args.rk_steps, "steps": args.rk_steps,
                              "stage_algorithmic_bytes": stage_bytes,
+                             "stage_bytes_note": "mean over the 4 Horner stages: weights + column ids, v and u "
+                                                 "read once (v = u in stage 1), out written once",
+                             "stage_GBps_without_u": args.rk_steps * (4 * nnz * (sz + 4) + 8 * N * F * sz)
+                                                     / (ms * 1e-3) / 1e9,
                              "stage_algorithmic_GBps": gbps, "stage_frac_of_hbm": gbps / hbm,
                              "stage_fma_TFLOPs": 4 * args.rk_steps * 2.0 * nnz * F / (ms * 1e-3) / 1e12,
                              "finite": bool(torch.isfinite(u).all().item())}
@@ -789,7 +795,8 @@ def rk4_block(r):
             "rho_dt_nominal", "stable_at_nominal_dt", "dt_used", "drift_f32_vs_f64", "hbm_peak_GBps")
     blk = {k: r[k] for k in keys}
     for p in ("f64", "f32"):
-        blk[p] = {k: r[p][k] for k in ("ms_per_step", "steps", "stage_algorithmic_GBps", "stage_frac_of_hbm",
+        blk[p] = {k: r[p][k] for k in ("ms_per_step", "steps", "stage_algorithmic_bytes", "stage_algorithmic_GBps",
+                                       "stage_frac_of_hbm", "stage_GBps_without_u", "stage_bytes_note",
                                        "stage_fma_TFLOPs", "finite")}
     return blk
 

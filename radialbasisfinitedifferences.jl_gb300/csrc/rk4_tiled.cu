@@ -382,12 +382,23 @@ struct TileMeta {
 #ifndef RBFFD_TILE_UNROLL
 #define RBFFD_TILE_UNROLL 2
 #endif
-constexpr int kTileUnroll = RBFFD_TILE_UNROLL;
+// 32 and 64 fields: each half-warp takes every other column (0: the whole warp per column).
+#ifndef RBFFD_TILE_CW2
+#define RBFFD_TILE_CW2 1
+#endif
+#ifndef RBFFD_TILE_UNROLL_CW2
+#define RBFFD_TILE_UNROLL_CW2 1
+#endif
+constexpr int kTileUnroll = RBFFD_TILE_UNROLL, kTileUnrollCW2 = RBFFD_TILE_UNROLL_CW2;
 template <int F>
 __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : RBFFD_TILE_MINB)) rk4_tile_stage_kernel(StageArgs s)
 {
     extern __shared__ __align__(128) unsigned char ts_smem[];
-    constexpr int FPL = F >= 32 ? F / 32 : 1, Q4 = F / 4;
+    // CW columns in flight per warp (one per half-warp when 2), LPC lanes per column, FPL
+    // fields per lane
+    constexpr int CW = (RBFFD_TILE_CW2 && (F == 32 || F == 64)) ? 2 : 1, LPC = 32 / CW;
+    constexpr int FPL = F >= LPC ? F / LPC : 1, Q4 = F / 4;
+    constexpr int kUnroll = CW == 2 ? kTileUnrollCW2 : kTileUnroll;
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     const TileOp &t = s.t;
     float *fb = reinterpret_cast<float *>(ts_smem);
@@ -398,8 +409,9 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : RBFFD_TILE_MINB)) r
     float *vref = reinterpret_cast<float *>(ts_smem + s.vrofs);
     int *goff = reinterpret_cast<int *>(ts_smem + s.gofs);
     int *refrow = goff + NGRP + 1;
-    const bool lact = lane * FPL < F;  // F < 32: only the first F lanes hold fields
-    const int lofs = lact ? lane * FPL : 0;
+    const int cl = lane & (LPC - 1);
+    const bool lact = cl * FPL < F;  // F < 32: only the first F lanes hold fields
+    const int lofs = lact ? cl * FPL : 0;
     int64_t tile = blockIdx.x;
     if (tile >= t.ntile) return;
     TileMeta cur;
@@ -424,51 +436,132 @@ __global__ void __launch_bounds__(32 * NGRP, (F >= 128 ? 2 : RBFFD_TILE_MINB)) r
         __syncthreads();  // the tile is in shared memory; its ids and offsets are consumed
         if (nxt < t.ntile) cur.store(t, ids, goff, refrow, s.u);  // read after the next barrier
         {
+            // With CW = 2 the two half-warps take alternate columns of the group (j + half,
+            // j + half + 2 of each block of four), so that a column's field row and weights
+            // are read by 16 lanes; their partial sums are added at the end, half 0 finishing
+            // rows 0-3 and half 1 rows 4-7.  The s_i v_ref term enters through half 0 only.
+            const int half = CW == 2 ? lane >> 4 : 0;
             const Fv<FPL> vr = ld_fields<FPL>(vref + lofs);
-            float acc[TG][FPL];
+            float rs[TG];
 #pragma unroll
-            for (int r = 0; r < TG; r++) {
-                const float rs = __int_as_float(rinfo[g * TG + r].y);
-#pragma unroll
-                for (int f = 0; f < FPL; f++) acc[r][f] = rs * vr.a[f];
-            }
+            for (int r = 0; r < TG; r++) rs[r] = half == 0 ? __int_as_float(rinfo[g * TG + r].y) : 0.0f;
             const uint4 *sl4 = reinterpret_cast<const uint4 *>(gsl + c0);
             const float4 *w4 = reinterpret_cast<const float4 *>(gwt + (size_t)c0 * TG);
             const float *fbl = fb + lofs;
-#pragma unroll kTileUnroll
+            // Packed FP32: one fma.rn.f32x2 updates two rows.  The weights of rows (2i, 2i+1)
+            // are adjacent in the group's weight record, so they form a register pair as
+            // loaded.  With two or more fields per lane, A holds (row 2i field 2e, row 2i+1
+            // field 2e+1) and B (row 2i field 2e+1, row 2i+1 field 2e), so that the column's
+            // differences (d_2e, d_2e+1) and their swap serve all row pairs; with one field per
+            // lane the difference is duplicated.
+            constexpr int RP = TG / 2, NP = FPL >= 2 ? FPL / 2 : 1;
+            float2 A[RP][NP], B[RP][NP];
+            float2 nv[NP];
+#pragma unroll
+            for (int e = 0; e < NP; e++) {
+                if constexpr (FPL >= 2) {
+                    nv[e] = make_float2(-vr.a[2 * e], -vr.a[2 * e + 1]);
+#pragma unroll
+                    for (int i = 0; i < RP; i++) {
+                        A[i][e] = make_float2(rs[2 * i] * vr.a[2 * e], rs[2 * i + 1] * vr.a[2 * e + 1]);
+                        B[i][e] = make_float2(rs[2 * i] * vr.a[2 * e + 1], rs[2 * i + 1] * vr.a[2 * e]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < RP; i++) A[i][e] = make_float2(rs[2 * i] * vr.a[0], rs[2 * i + 1] * vr.a[0]);
+                }
+            }
+            auto column = [&](const Fv<FPL> &xq, const float4 wa, const float4 wb) {
+                const float2 wp[RP] = {make_float2(wa.x, wa.y), make_float2(wa.z, wa.w), make_float2(wb.x, wb.y),
+                                       make_float2(wb.z, wb.w)};
+#pragma unroll
+                for (int e = 0; e < NP; e++) {
+                    if constexpr (FPL >= 2) {
+                        const float2 d = __fadd2_rn(make_float2(xq.a[2 * e], xq.a[2 * e + 1]), nv[e]);
+                        const float2 ds = make_float2(d.y, d.x);
+#pragma unroll
+                        for (int i = 0; i < RP; i++) {
+                            A[i][e] = __ffma2_rn(wp[i], d, A[i][e]);
+                            B[i][e] = __ffma2_rn(wp[i], ds, B[i][e]);
+                        }
+                    } else {
+                        const float d = xq.a[0] - vr.a[0];
+                        const float2 dd = make_float2(d, d);
+#pragma unroll
+                        for (int i = 0; i < RP; i++) A[i][e] = __ffma2_rn(wp[i], dd, A[i][e]);
+                    }
+                }
+            };
+#pragma unroll kUnroll
             for (int j = 0; j < cn; j += 4) {
                 const uint4 s4 = sl4[j >> 2];
-                const uint32_t sc[4] = {s4.x, s4.y, s4.z, s4.w};
-                Fv<FPL> x[4];
+                if constexpr (CW == 2) {
+                    const uint32_t sc[2] = {half ? s4.y : s4.x, half ? s4.w : s4.z};
+                    Fv<FPL> x[2];
 #pragma unroll
-                for (int q = 0; q < 4; q++) x[q] = ld_fields<FPL>(fbl + sc[q]);
+                    for (int q = 0; q < 2; q++) x[q] = ld_fields<FPL>(fbl + sc[q]);
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float4 wa = w4[2 * (j + q)], wb = w4[2 * (j + q) + 1];
-                    const float w[TG] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+                    for (int q = 0; q < 2; q++) {
+                        const int col = j + half + 2 * q;
+                        column(x[q], w4[2 * col], w4[2 * col + 1]);
+                    }
+                } else {
+                    const uint32_t sc[4] = {s4.x, s4.y, s4.z, s4.w};
+                    Fv<FPL> x[4];
 #pragma unroll
-                    for (int f = 0; f < FPL; f++) {
-                        const float d = x[q].a[f] - vr.a[f];
+                    for (int q = 0; q < 4; q++) x[q] = ld_fields<FPL>(fbl + sc[q]);
 #pragma unroll
-                        for (int r = 0; r < TG; r++) acc[r][f] = fmaf(w[r], d, acc[r][f]);
+                    for (int q = 0; q < 4; q++) column(x[q], w4[2 * (j + q)], w4[2 * (j + q) + 1]);
+                }
+            }
+            float acc[TG][FPL];
+#pragma unroll
+            for (int i = 0; i < RP; i++) {
+#pragma unroll
+                for (int e = 0; e < NP; e++) {
+                    if constexpr (FPL >= 2) {
+                        acc[2 * i][2 * e] = A[i][e].x;
+                        acc[2 * i + 1][2 * e + 1] = A[i][e].y;
+                        acc[2 * i][2 * e + 1] = B[i][e].x;
+                        acc[2 * i + 1][2 * e] = B[i][e].y;
+                    } else {
+                        acc[2 * i][0] = A[i][e].x;
+                        acc[2 * i + 1][0] = A[i][e].y;
+                    }
+                }
+            }
+            // rows this lane finishes: all 8 (CW = 1) or 4 of them (CW = 2)
+            constexpr int NR = TG / CW;
+            float fin[NR][FPL];
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+#pragma unroll
+                for (int f = 0; f < FPL; f++) {
+                    if constexpr (CW == 2) {
+                        const float send = half ? acc[r][f] : acc[r + NR][f];
+                        const float keep = half ? acc[r + NR][f] : acc[r][f];
+                        fin[r][f] = keep + __shfl_xor_sync(RBFFD_FULL, send, 16);
+                    } else {
+                        fin[r][f] = acc[r][f];
                     }
                 }
             }
             if (lact) {
-                // all 8 rows' u loads issued before the first store
-                int4 ri[TG];
-                Fv<FPL> uu[TG];
+                // all rows' u loads issued before the first store
+                const int rb = g * TG + half * NR;
+                int4 ri[NR];
+                Fv<FPL> uu[NR];
 #pragma unroll
-                for (int r = 0; r < TG; r++) {
-                    ri[r] = rinfo[g * TG + r];
+                for (int r = 0; r < NR; r++) {
+                    ri[r] = rinfo[rb + r];
                     uu[r] = ld_fields<FPL>(s.u + (size_t)(ri[r].x < 0 ? 0 : ri[r].x) * F + lofs);
                 }
 #pragma unroll
-                for (int r = 0; r < TG; r++) {
+                for (int r = 0; r < NR; r++) {
                     if (ri[r].x < 0) continue;
                     Fv<FPL> res;
 #pragma unroll
-                    for (int f = 0; f < FPL; f++) res.a[f] = ri[r].w ? uu[r].a[f] : fmaf(s.c, acc[r][f], uu[r].a[f]);
+                    for (int f = 0; f < FPL; f++) res.a[f] = ri[r].w ? uu[r].a[f] : fmaf(s.c, fin[r][f], uu[r].a[f]);
                     st_fields<FPL>(s.out + (size_t)ri[r].x * F + lofs, res);
                 }
             }
