@@ -464,11 +464,27 @@ int fallback_wpb(rbffd_handle *h, size_t per_warp)
 
 void set_handleless_error(const std::string &msg) { g_create_error = msg; }
 
+// Closed-form right-hand sides for r^3 with Dx/Dy/Lap in the register Schur kernel (0: the
+// term table for every operator).
+#ifndef RBFFD_RHS_CLOSED
+#define RBFFD_RHS_CLOSED 1
+#endif
 bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, std::string *err)
 {
     memset(t, 0, sizeof(*t));
     t->nops = nops;
     t->p = p;
+    int closed = 1;
+    for (int q = 0; q < nops; q++) {
+        if (ops[q] == RBFFD_OP_DX || ops[q] == RBFFD_OP_DY)
+            closed |= 2;
+        else if (ops[q] == RBFFD_OP_LAP)
+            closed |= 4;
+        else
+            closed = 0;  // any other operator: the term table
+        if (!closed) break;
+    }
+    t->r3_grad_lap = (RBFFD_RHS_CLOSED && p == 3) ? closed : 0;
     for (int q = 0; q < nops; q++) {
         OpDesc &d = t->op[q];
         int code = ops[q];

@@ -44,6 +44,10 @@ struct OpDesc {
 struct OpTable {
     int nops;
     int p;
+    // Nonzero when p = 3 and every operator is Dx, Dy or Lap: the register Schur kernel then
+    // forms their right-hand sides from closed forms instead of the term table.  Bit 0 set,
+    // bit 1: some Dx or Dy, bit 2: some Lap.
+    int r3_grad_lap;
     OpDesc op[RBFFD_MAX_OPS];
 };
 

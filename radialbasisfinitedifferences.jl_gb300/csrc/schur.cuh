@@ -111,7 +111,7 @@ __host__ __device__ inline SchurLayout make_schur_layout(int SP, int SM, int max
     L.prow = o;
     o += al16(sizeof(float) * (wmax + 4));
     L.sc = o;
-    o += al16(sizeof(double) * 2 * nops);
+    o += al16(sizeof(double) * (2 * nops + 2));
     // union: setup arrays
     size_t u = o;
     L.x32 = u;
@@ -833,6 +833,7 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
 {
     const int r = ops.nops;
     const bool at0 = is_zero64(yx) && is_zero64(yy);
+    const int closed = ops.r3_grad_lap;
     for (int i = lane; i < n; i += 32) {
         // y~ - x~_i; at the centre (the collocated case) the negation is a sign flip on the
         // integer pipe instead of an FP64 subtraction from zero
@@ -843,6 +844,18 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
         double y0;
         const double rr = sqrt_nr(r2, y0);
         const double rinv = need_rinv ? recip_nr(rr, y0) : 0.0;
+        if (closed) {
+            // d/dx r^3 = 3 x r, d/dy r^3 = 3 y r, and sx^2 d2/dx2 r^3 + sy^2 d2/dy2 r^3
+            // = (3 (2 sx^2 + sy^2) x^2 + 3 (sx^2 + 2 sy^2) y^2) / r (with r^2 = x^2 + y^2):
+            // 8 FP64 operations per node for Dx, Dy and Lap after r and 1/r instead of 17
+            const double t3 = (closed & 2) ? 3.0 * rr : 0.0;
+            const double lap = (closed & 4) ? fma(sc[2 * r] * cx, cx, (sc[2 * r + 1] * cy) * cy) * rinv : 0.0;
+            for (int q = 0; q < r; q++) {
+                const OpDesc &od = ops.op[q];
+                B[i * r + q] = od.ncomp == 2 ? lap : t3 * (od.c[0].a ? cx : cy);
+            }
+            continue;
+        }
         for (int q = 0; q < r; q++) {
             const OpDesc &od = ops.op[q];
             double v = 0.0;
@@ -865,6 +878,22 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
             }
             B[i * r + q] = v;
         }
+    }
+    if (closed && at0) {
+        // the polynomial rows at the centre: 1 at x (Dx) or y (Dy); 2 sx^2 at x^2 and 2 sy^2
+        // at y^2 (Lap); zero elsewhere
+        for (int l = lane; l < m; l += 32)
+            for (int q = 0; q < r; q++) {
+                const OpDesc &od = ops.op[q];
+                double v = 0.0;
+                if (od.ncomp == 2)
+                    v = l == 3 ? twice64(sc[2 * q]) : l == 5 ? twice64(sc[2 * q + 1]) : 0.0;
+                else if (l == (od.c[0].a ? 1 : 2))
+                    v = 1.0;
+                B[(n + l) * r + q] = v;
+            }
+        __syncwarp();
+        return;
     }
     for (int l = lane; l < m; l += 32) {
         int t = 0, rem = l;
@@ -997,6 +1026,10 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
         if (lane < 2 * r) {
             const int q = lane >> 1, c = lane & 1;
             if (c < ops.op[q].ncomp) sc[lane] = ipow(sx, ops.op[q].c[c].a) * ipow(sy, ops.op[q].c[c].b);
+        } else if ((ops.r3_grad_lap & 4) && lane < 2 * r + 2) {
+            // the closed-form Lap of r^3: 3 (2 sx^2 + sy^2) and 3 (sx^2 + 2 sy^2)
+            const double sx2 = sx * sx, sy2 = sy * sy;
+            sc[lane] = 3.0 * (lane == 2 * r ? twice64(sx2) + sy2 : sx2 + twice64(sy2));
         }
         __syncwarp();
         RegRows<SP> RP;

@@ -90,6 +90,16 @@ __device__ __forceinline__ float warp_max_f(float v)
 }
 
 __device__ __forceinline__ bool is_zero64(double x) { return abs_key(x) == 0ull; }
+// 2 x for a normal double (exponent field + 1, integer pipe); zero, subnormal and
+// non-finite x take the FP64 addition.
+__device__ __forceinline__ double twice64(double x)
+{
+    const int hi = __double2hiint(x);
+    const unsigned ex = ((unsigned)hi >> 20) & 0x7ffu;
+    if (ex == 0u || ex >= 0x7feu) return x + x;
+    return __hiloint2double(hi + (1 << 20), __double2loint(x));
+}
+
 // -x by flipping the sign bit (integer pipe; exact, like the FP64 negation)
 __device__ __forceinline__ double neg64(double x)
 {
