@@ -63,6 +63,13 @@ __device__ __forceinline__ float sel_f32(bool c, float a, float b)
     return r;
 }
 
+// floor(t / d) for 0 <= t < 2^12 and 1 <= d <= 128 by a multiply and a shift, g = div19_magic(d)
+// = ceil(2^19 / d) (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994: 19 = 12 + ceil(log2 d) bits make the quotient exact), instead of
+// the instruction sequence of a run-time integer division.
+__host__ __device__ inline uint32_t div19_magic(int d) { return (524288u + (uint32_t)d - 1u) / (uint32_t)d; }
+__device__ __forceinline__ int div19(int t, uint32_t g) { return (int)(((uint32_t)t * g) >> 19); }
+
 template <int S>
 struct RegRows {
     static constexpr int NS = (S + 31) / 32;
@@ -260,16 +267,14 @@ __device__ __forceinline__ bool reg_gj(RegRows<S> &R, int s, int *perm, float *d
 
 // G = Phi^-1 P, S = -P' G, Sinv = S^-1 (natural order).  Returns false on a singular S.
 template <int SP, int SM>
-__device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m, const int *permP, const float *P32,
-                                            float *Pp, float *G, int ldg, float *Sm, float *Sinv, int lds,
-                                            int *permS, float *dinvS, float *prow, int lane)
+__device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m, uint32_t gm, const int *permP,
+                                            const float *P32, float *Pp, float *G, int ldg, float *Sm, float *Sinv,
+                                            int lds, int *permS, float *dinvS, float *prow, int lane)
 {
     constexpr int NS = RegRows<SP>::NS;
     const int n4 = (n + 3) & ~3;
-    for (int t = lane; t < m * n4; t += 32) {
-        const int l = t / n4, jj = t - l * n4;
-        Pp[t] = jj < n ? P32[permP[jj] * m + l] : 0.0f;
-    }
+    for (int l = 0; l < m; l++)
+        for (int jj = lane; jj < n4; jj += 32) Pp[l * n4 + jj] = jj < n ? P32[permP[jj] * m + l] : 0.0f;
     __syncwarp();
 #pragma unroll
     for (int k = 0; k < NS; k++) {
@@ -314,7 +319,7 @@ __device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m,
     }
     __syncwarp();
     for (int t = lane; t < m * m; t += 32) {
-        const int aa = t / m, bb = t - aa * m;
+        const int aa = div19(t, gm), bb = t - aa * m;
         float s0 = 0.0f, s1 = 0.0f;
         int i = 0;
         for (; i + 2 <= n; i += 2) {
@@ -353,7 +358,7 @@ __device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m,
 
 // R32 <- A^-1 R32 (s x r, row-major) through Phi^-1 (registers), G and Sinv.
 template <int SP, int RMAX>
-__device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int m, int r, const int *permP,
+__device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int m, int r, uint32_t gr, const int *permP,
                                               const float *G, int ldg, const float *Sinv, int lds, float *R32,
                                               float *U, float *Lam, float4 *bp, int lane)
 {
@@ -369,7 +374,7 @@ __device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int 
         bp[t] = make_float4(e[0], e[1], e[2], e[3]);
     }
     for (int e = lane; e < m * r; e += 32) {
-        const int l = e / r, q = e - l * r;
+        const int l = div19(e, gr), q = e - l * r;
         float u0 = R32[(n + l) * r + q], u1 = 0.0f;
         int i = 0;
         for (; i + 2 <= n; i += 2) {
@@ -382,7 +387,7 @@ __device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int 
     __syncwarp();
     // (2) lambda = Sinv u (shared memory); t = Phi^-1 r1 (registers)
     for (int e = lane; e < m * r; e += 32) {
-        const int l = e / r, q = e - l * r;
+        const int l = div19(e, gr), q = e - l * r;
         float v0 = 0.0f, v1 = 0.0f;
         int aa = 0;
         for (; aa + 2 <= m; aa += 2) {
@@ -439,7 +444,7 @@ __device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int 
         }
     }
     for (int e = lane; e < m * r; e += 32) {
-        const int l = e / r, q = e - l * r;
+        const int l = div19(e, gr), q = e - l * r;
         R32[(n + l) * r + q] = Lam[l * 4 * RQ + q];
     }
     __syncwarp();
@@ -493,7 +498,7 @@ __device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
 
 // NE (1 or 2) elements (i, q) of r = b - A x for the Phi rows, elements e0 + lane + 32 u.
 template <int NE>
-__device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r,
+__device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r, uint32_t gr,
                                                   double *B, const double *X, float *R32, int e0, bool store_r,
                                                   int lane)
 {
@@ -504,7 +509,7 @@ __device__ __forceinline__ void residual_phi_rows(const double *phiP, const doub
     for (int u = 0; u < NE; u++) {
         ee[u] = e0 + lane + 32 * u;
         const int ec = ee[u] < tot ? ee[u] : tot - 1;
-        ii[u] = ec / r;
+        ii[u] = div19(ec, gr);
         qq[u] = ec - ii[u] * r;
         off[u] = tri_off(ii[u]);
         a0[u] = B[ec];
@@ -556,18 +561,18 @@ __device__ __forceinline__ void residual_phi_rows(const double *phiP, const doub
 // products, lane-per-element: ceil(n r / 32) lane-full passes
 // of n + m FMAs for the Phi rows (two passes interleaved per lane), one pass of n FMAs per 32
 // elements for the P' rows.  Phi is read from its packed lower triangle.
-__device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r,
+__device__ __forceinline__ void residual_schur(const double *phiP, const double *P, int n, int m, int r, uint32_t gr,
                                               double *B, const double *X, float *R32, bool store_r, int lane)
 {
     const int tot = n * r;
     for (int e0 = 0; e0 < tot; e0 += 64) {
         if (e0 + 32 < tot)
-            residual_phi_rows<2>(phiP, P, n, m, r, B, X, R32, e0, store_r, lane);
+            residual_phi_rows<2>(phiP, P, n, m, r, gr, B, X, R32, e0, store_r, lane);
         else
-            residual_phi_rows<1>(phiP, P, n, m, r, B, X, R32, e0, store_r, lane);
+            residual_phi_rows<1>(phiP, P, n, m, r, gr, B, X, R32, e0, store_r, lane);
     }
     for (int e = lane; e < m * r; e += 32) {
-        const int l = e / r, q = e - l * r;
+        const int l = div19(e, gr), q = e - l * r;
         double a0 = B[(n + l) * r + q], a1 = 0.0;
         int jj = 0;
         for (; jj + 2 <= n; jj += 2) {
@@ -629,7 +634,7 @@ __device__ __forceinline__ void split_at(const double *a, int ad, float &hi, flo
 // an FP64 residual.  B holds r_old as (hi, lo) pairs and receives r_new; R32 receives hi.  Phi rows lane-per-row (the split of Phi_ij shared by the row's
 // operators), P' rows lane-per-element.  PRE: Phi and P hold their splits already.
 template <int SP, int SM, int RMAX, bool PRE>
-__device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, double *B,
+__device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, uint32_t gr, double *B,
                                             float *R32, int lane)
 {
     constexpr int NS = RegRows<SP>::NS;
@@ -679,7 +684,7 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
         th[u] = tl[u] = 0.0f;
         const int e = lane + 32 * u;
         if (e < m * r) {
-            const int l = e / r, q = e - l * r;
+            const int l = div19(e, gr), q = e - l * r;
             for (int jj = 0; jj < n; jj++) {
                 float ah, al;
                 split_at<PRE>(P, jj * m + l, ah, al);
@@ -985,6 +990,7 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
     float *Lam = (float *)(base + L.Lam);
     float4 *bp = (float4 *)(base + L.bp);
     const int r = ops.nops, p = ops.p, ldg = L.ldg, lds = L.lds;
+    const uint32_t gr = div19_magic(r);
 
     const float tol32 = f64_to_f32(a.refine_tol);
     bool need_rinv = false;
@@ -1035,7 +1041,7 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
         RegRows<SP> RP;
         fill_phi_rows<SP>(RP, x32, n, p, lane);
         bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
-        if (ok) ok = build_schur<SP, SM>(RP, n, m, permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
+        if (ok) ok = build_schur<SP, SM>(RP, n, m, div19_magic(m), permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
         bool fallback = !ok;
         if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, xf, lane);
         int64_t r0, r1;
@@ -1058,17 +1064,17 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
                     for (int e = lane; e < s * r; e += 32) R32[e] = f64_to_f32(B[e]);
                     __syncwarp();
                 } else if (it == 1) {
-                    residual_schur(phiP, P, n, m, r, B, X, R32, true, lane);
+                    residual_schur(phiP, P, n, m, r, gr, B, X, R32, true, lane);
                 } else if (one_row) {
                     if (!presplit) {
                         presplit_phi_p(phiP, P, n, m, lane);
                         presplit = true;
                     }
-                    residual_df<SP, SM, RMAX, true>(phiP, P, n, m, r, B, R32, lane);
+                    residual_df<SP, SM, RMAX, true>(phiP, P, n, m, r, gr, B, R32, lane);
                 } else {
-                    residual_df<SP, SM, RMAX, false>(phiP, P, n, m, r, B, R32, lane);
+                    residual_df<SP, SM, RMAX, false>(phiP, P, n, m, r, gr, B, R32, lane);
                 }
-                schur_correct<SP, RMAX>(RP, n, m, r, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
+                schur_correct<SP, RMAX>(RP, n, m, r, gr, permP, G, ldg, Sinv, lds, R32, U, Lam, bp, lane);
                 // x0 is kept as FP64 for the FP64 first residual; from the first update on, x is
                 // a double-float pair in the same 8 bytes of each element.
                 unsigned dkey = 0u, xkey = 0u;
