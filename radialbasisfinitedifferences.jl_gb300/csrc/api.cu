@@ -104,6 +104,8 @@ struct Arena {
     }
 };
 
+__global__ void set_i64(int64_t *a, int64_t v) { *a = v; }
+
 __global__ void iota_i32(int32_t *a, int64_t n, int64_t base)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -731,11 +733,7 @@ static int opset_build(rbffd_handle *h, const rbffd_problem *pb, int unscaled, r
     CK(cudaEventRecord(h->ev[2], st));
     Flags *dflags;
     CK(tmp.zeros(&dflags, 1));
-    {
-        int64_t big = INT64_MAX;
-        CK(cudaMemcpyAsync(&dflags->first_bad, &big, sizeof(big), cudaMemcpyHostToDevice, st));
-        CK(cudaStreamSynchronize(st));
-    }
+    set_i64<<<1, 1, 0, st>>>(&dflags->first_bad, INT64_MAX);  // stream-ordered: no host round trip
     // ---- nearest node of every row and the systems to factor
     int32_t *nn;  // rows
     int32_t *sys_node;
