@@ -42,6 +42,12 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 // lane need up to 255).  A CTA may hold all of an SM's warps (512 or 256 threads).
 #define RBFFD_SCHUR_MAX_THREADS(SP) ((SP) <= 32 ? 512 : 256)
 
+// Double-float residual sums of the Phi and P rows on pairs of operators in packed FP32
+// (0: one operator at a time).
+#ifndef RBFFD_DF_PACKED
+#define RBFFD_DF_PACKED 1
+#endif
+
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
 template <int B, int E, typename F>
 __device__ __forceinline__ void static_for(F &&f)
@@ -601,6 +607,23 @@ __device__ __forceinline__ void df_mac(float a, float d, float &s_hi, float &s_l
     s_lo += err + e;
 }
 
+// df_mac on two sums at once (packed FP32, fma.rn.f32x2 and relatives): (sh, sl) += a (d.x, d.y)
+// + al (d.x, d.y), with a2 = (a, a), na2 = (-a, -a), al2 = (al, al).  Differences x - y are
+// fma(y, -1, x), exact like the subtraction.  The same operations as df_mac followed by
+// sl = fmaf(al, d, sl) on each half, except that the product's error enters sl after the
+// TwoSum error instead of with it.
+__device__ __forceinline__ void df_mac2(float2 a2, float2 na2, float2 al2, float2 d, float2 &sh, float2 &sl)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 p = __fmul2_rn(a2, d);
+    const float2 ne = __ffma2_rn(na2, d, p);  // -(a d - p), exact
+    const float2 s = __fadd2_rn(sh, p);
+    const float2 bb = __ffma2_rn(sh, m1, s);                                            // s - sh
+    const float2 err = __fadd2_rn(__ffma2_rn(__ffma2_rn(bb, m1, s), m1, sh), __ffma2_rn(bb, m1, p));  // TwoSum error
+    sh = s;
+    sl = __ffma2_rn(al2, d, __ffma2_rn(ne, m1, __fadd2_rn(sl, err)));
+}
+
 // The packed Phi and P of a system rewritten in place as their double-float splits (float2
 // (hi, lo) in the same 8 bytes per element), for the later residuals of a system with a single
 // evaluation row: its FP64 first residual, the only user of the exact FP64 values, is done.
@@ -639,6 +662,53 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
 {
     constexpr int NS = RegRows<SP>::NS;
     float sh[NS][RMAX], sl[NS][RMAX];
+#if RBFFD_DF_PACKED
+    // Phi and P rows: the operators' sums in pairs (q, q + 1); a pair past r computes on zeros
+    constexpr int QP = (RMAX + 1) / 2;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        float2 SH[QP], SL[QP];
+#pragma unroll
+        for (int u = 0; u < QP; u++) SH[u] = SL[u] = make_float2(0.0f, 0.0f);
+        if (32 * k < n) {
+            const int i = lane + 32 * k;
+            const int ii = i < n ? i : n - 1;
+            const int offi = tri_off(ii);
+            auto column = [&](float ah, float al, const float *dj) {
+                const float2 a2 = make_float2(ah, ah), na2 = make_float2(-ah, -ah), al2 = make_float2(al, al);
+#pragma unroll
+                for (int u = 0; u < QP; u++) {
+                    if (2 * u < r) {
+                        const float2 d = make_float2(dj[2 * u], 2 * u + 1 < r ? dj[2 * u + 1] : 0.0f);
+                        df_mac2(a2, na2, al2, d, SH[u], SL[u]);
+                    }
+                }
+            };
+            int offj = 0;
+            for (int jj = 0; jj < n; jj++) {
+                const int ad = jj <= ii ? offi + jj : offj + ii;
+                offj += jj + 1;
+                float ah, al;
+                split_at<PRE>(phiP, ad, ah, al);
+                column(ah, al, R32 + jj * r);
+            }
+            for (int l = 0; l < m; l++) {
+                float ah, al;
+                split_at<PRE>(P, ii * m + l, ah, al);
+                column(ah, al, R32 + (n + l) * r);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < QP; u++) {
+            sh[k][2 * u] = SH[u].x;
+            sl[k][2 * u] = SL[u].x;
+            if (2 * u + 1 < RMAX) {
+                sh[k][2 * u + 1] = SH[u].y;
+                sl[k][2 * u + 1] = SL[u].y;
+            }
+        }
+    }
+#else
 #pragma unroll
     for (int k = 0; k < NS; k++) {
 #pragma unroll
@@ -677,6 +747,7 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
             }
         }
     }
+#endif
     constexpr int PE = (SM * RMAX + 31) / 32;  // P' elements per lane (m r <= SM RMAX)
     float th[PE], tl[PE];
 #pragma unroll
