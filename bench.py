@@ -512,13 +512,14 @@ def run_ours(args):
     manu = manufactured_errors(pkg, h)
     m = 10
     s_ = n + m
-    # FP64 work of the mixed solve per system: the monomials of P, the right-hand sides, the
-    # first refinement residual 2 (s^2 - m^2) r and the FP64 solution updates.  The pairwise
-    # Phi = r^3 is formed in exact fixed-point integer arithmetic and the later residuals are
-    # double-float FP32 products: neither is FP64 work and neither is counted.
+    # FP64 work of the mixed solve per system: the monomials of P (7 products per node at
+    # degree 3), the closed-form right-hand sides of Dx/Dy/Lap for r^3 (29 flops per node: r^2,
+    # r and 1/r by Newton steps, 3r, the three values), the first refinement residual
+    # 2 (s^2 - m^2) r and the output (hi + lo, and the scale of Dx/Dy: 5 per node).  The
+    # pairwise Phi = r^3 is exact fixed-point integer work, and the later residuals and the
+    # solution updates are double-float FP32: none of them is FP64 work or counted.
+    fp64_flops_sys = 7 * n + 29 * n + 2 * (s_ * s_ - m * m) * 3 + 5 * n
     hist = mixed_stats["refine_hist"]
-    nres = sum(i * c for i, c in enumerate(hist)) / max(1, sum(hist))
-    fp64_flops_sys = n * m + n * 3 * 12 + 2 * (s_ * s_ - m * m) * 3 + (nres + 1) * s_ * 3
     solve_ach = rows_per * fp64_flops_sys / (solve_ms * 1e-3) / 1e12
     hbm, hbm_src = hbm_peak()
     out = {
@@ -569,8 +570,9 @@ def run_ours(args):
             "frac": solve_ach / fp64_peak.value if fp64_peak.value else None,
             "traffic": NCU_TRAFFIC["solve_bytes_per_system"] * rows_per,
             "traffic_note": "bytes per launch, ncu on 512x512 scaled by systems (stencil gathers + CSR output)",
-            "note": "FP64 work of the mixed solve (P monomials, RHS, first residual, updates; Phi = r^3 is exact "
-                    "fixed-point integer work and the later residuals double-float FP32) over the kernel's "
+            "note": "FP64 work of the mixed solve (P monomials, closed-form right-hand sides, first residual, "
+                    "output; Phi = r^3 is exact fixed-point integer work, the later residuals and the updates "
+                    "double-float FP32) over the kernel's "
                     "event-timed duration, against the measured FP64 FMA peak (rbffd_measure_fma_peaks); the kernel "
                     "is latency/issue-bound with the FP64 pipe one of several busy units (profiles/)",
         },
