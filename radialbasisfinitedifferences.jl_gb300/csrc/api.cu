@@ -487,6 +487,9 @@ bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, st
         if (!closed) break;
     }
     t->r3_grad_lap = (RBFFD_RHS_CLOSED && p == 3) ? closed : 0;
+    bool hv4 = nops > 0;
+    for (int q = 0; q < nops; q++) hv4 = hv4 && (ops[q] == RBFFD_OP_DXK || ops[q] == RBFFD_OP_DYK);
+    t->r5_hv4 = RBFFD_RHS_CLOSED && p == 5 && k_deriv == 4 && hv4;
     for (int q = 0; q < nops; q++) {
         OpDesc &d = t->op[q];
         int code = ops[q];

@@ -48,6 +48,9 @@ struct OpTable {
     // forms their right-hand sides from closed forms instead of the term table.  Bit 0 set,
     // bit 1: some Dx or Dy, bit 2: some Lap.
     int r3_grad_lap;
+    // 1 when p = 5, K = 4 and every operator is Dxk or Dyk (the hyperviscosity pair of the
+    // time-stepping example): closed forms likewise.
+    int r5_hv4;
     OpDesc op[RBFFD_MAX_OPS];
 };
 

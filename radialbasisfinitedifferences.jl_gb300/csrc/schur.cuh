@@ -932,6 +932,17 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
             }
             continue;
         }
+        if (ops.r5_hv4) {
+            // d4/dx4 r^5 = -15 x^4 / r^3 + 90 x^2 / r + 45 r = 15 r (3 + u (6 - u)), u = x^2 / r^2
+            // (u in [0, 1]: no cancellation): 5 FP64 operations per operator instead of 13
+            const double rinv2 = rinv * rinv, r15 = 15.0 * rr;
+            for (int q = 0; q < r; q++) {
+                const double c = ops.op[q].c[0].a ? cx : cy;
+                const double u = (c * c) * rinv2;
+                B[i * r + q] = r15 * fma(u, 6.0 - u, 3.0);
+            }
+            continue;
+        }
         for (int q = 0; q < r; q++) {
             const OpDesc &od = ops.op[q];
             double v = 0.0;
@@ -954,6 +965,13 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
             }
             B[i * r + q] = v;
         }
+    }
+    if (ops.r5_hv4 && at0) {
+        // the polynomial rows at the centre: 4! at x^4 (Dxk) or y^4 (Dyk), zero elsewhere
+        for (int l = lane; l < m; l += 32)
+            for (int q = 0; q < r; q++) B[(n + l) * r + q] = l == (ops.op[q].c[0].a ? 10 : 14) ? 24.0 : 0.0;
+        __syncwarp();
+        return;
     }
     if (closed && at0) {
         // the polynomial rows at the centre: 1 at x (Dx) or y (Dy); 2 sx^2 at x^2 and 2 sy^2

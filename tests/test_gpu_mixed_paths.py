@@ -7,6 +7,9 @@
   K = 4 (the configuration of the time-stepping example, examples/adv_diff_test.jl:95-101).
 * The shared-memory mixed kernel, which takes what the register kernels do not: stencils of
   more than 64 nodes, more than 32 monomials, or more than 8 operators.
+* The closed-form right-hand sides of the register kernel (PHS r^3 with every operator in
+  {Dx, Dy, Lap}): operator subsets and orders, stencil sizes of each register instantiation,
+  and evaluation points off the nodes (rows that share a nearest node's factorisation).
 
 Bars as in test_gpu_parity.py: 1e-9 row-relative for mixed weights of well-conditioned
 systems (PHS r^3, degree <= 3), 5e-9 for r^5 or degree >= 4 (where the oracle's explicit
@@ -203,3 +206,42 @@ def test_loose_refine_tol_keeps_its_promise(pkg, orc, gpu, tol):
             st = s.stats.as_dict()
             assert st["refine_hist"][1] == 0, st
             check_against_oracle(s, ref, ops, n, max(MIXED_TOL, 10 * tol))
+
+
+@pytest.mark.parametrize("ops", [("Lap",), ("Dx",), ("Dy", "Lap"), ("Lap", "Dx"), ("Lap", "Dy", "Dx")])
+@pytest.mark.parametrize("n,deg", [(30, 3), (45, 4), (60, 5)])
+def test_closed_form_rhs_operator_subsets(pkg, orc, gpu, ops, n, deg):
+    X = grid(pkg, 48, seed=8)
+    ref = orc.generate(X, X, 3, n, deg, ops)
+    with pkg.OperatorSet(X, None, 3, n, deg, ops=ops, precision="mixed") as s:
+        check_against_oracle(s, ref, ops, n, tol_for(3, deg))
+
+
+def test_closed_form_rhs_noncollocated(pkg, orc, gpu):
+    X = grid(pkg, 40, seed=9)
+    Y = np.random.default_rng(10).uniform(0.02, 0.98, (3000, 2))
+    ops = ("Dx", "Dy", "Lap")
+    ref = orc.generate(X, Y, 3, 20, 3, ops)
+    with pkg.OperatorSet(X, Y, 3, 20, 3, ops=ops, precision="mixed") as s:
+        check_against_oracle(s, ref, ops, 20, MIXED_TOL)
+
+
+@pytest.mark.parametrize("ops", [("Dxk", "Dyk"), ("Dyk",), ("Dyk", "Dxk")])
+@pytest.mark.parametrize("n,deg", [(20, 2), (30, 3), (45, 4), (60, 5)])
+def test_closed_form_rhs_hyperviscosity_pair(pkg, orc, gpu, ops, n, deg):
+    """PHS r^5 with K = 4 and only Dxk/Dyk (the time-stepping example's pair) takes the closed
+    form d4/dx4 r^5 = 15 r (3 + 6 u - u^2), u = x^2 / r^2, and 4! at x^4 or y^4 in the
+    polynomial rows; degrees 4 and 5 have those monomials."""
+    X = grid(pkg, 48, seed=17)
+    ref = orc.generate(X, X, 5, n, deg, ops, k_deriv=4)
+    with pkg.OperatorSet(X, None, 5, n, deg, ops=ops, k_deriv=4, precision="mixed") as s:
+        check_against_oracle(s, ref, ops, n, tol_for(5, deg))
+
+
+def test_closed_form_rhs_hyperviscosity_noncollocated(pkg, orc, gpu):
+    X = grid(pkg, 40, seed=18)
+    Y = np.random.default_rng(19).uniform(0.02, 0.98, (3000, 2))
+    ops = ("Dxk", "Dyk")
+    ref = orc.generate(X, Y, 5, 30, 3, ops, k_deriv=4)
+    with pkg.OperatorSet(X, Y, 5, 30, 3, ops=ops, k_deriv=4, precision="mixed") as s:
+        check_against_oracle(s, ref, ops, 30, tol_for(5, 3))
