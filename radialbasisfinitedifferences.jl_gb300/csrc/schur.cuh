@@ -42,12 +42,6 @@ constexpr int PADROW = -1;  // pivot step of padding rows: never a pivot, never 
 // lane need up to 255).  A CTA may hold all of an SM's warps (512 or 256 threads).
 #define RBFFD_SCHUR_MAX_THREADS(SP) ((SP) <= 32 ? 512 : 256)
 
-// Double-float residual sums of the Phi and P rows on pairs of operators in packed FP32
-// (0: one operator at a time).
-#ifndef RBFFD_DF_PACKED
-#define RBFFD_DF_PACKED 1
-#endif
-
 // Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
 template <int B, int E, typename F>
 __device__ __forceinline__ void static_for(F &&f)
@@ -364,9 +358,9 @@ __device__ __forceinline__ bool build_schur(const RegRows<SP> &RP, int n, int m,
 
 // R32 <- A^-1 R32 (s x r, row-major) through Phi^-1 (registers), G and Sinv.
 template <int SP, int RMAX>
-__device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int m, int r, uint32_t gr, const int *permP,
-                                              const float *G, int ldg, const float *Sinv, int lds, float *R32,
-                                              float *U, float *Lam, float4 *bp, int lane)
+__device__ __forceinline__ void schur_correct(const RegRows<SP> &RP, int n, int m, int r, uint32_t gr,
+                                              const int *permP, const float *G, int ldg, const float *Sinv, int lds,
+                                              float *R32, float *U, float *Lam, float4 *bp, int lane)
 {
     constexpr int NS = RegRows<SP>::NS;
     constexpr int RQ = (RMAX + 3) / 4;
@@ -504,9 +498,9 @@ __device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
 
 // NE (1 or 2) elements (i, q) of r = b - A x for the Phi rows, elements e0 + lane + 32 u.
 template <int NE>
-__device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r, uint32_t gr,
-                                                  double *B, const double *X, float *R32, int e0, bool store_r,
-                                                  int lane)
+__device__ __forceinline__ void residual_phi_rows(const double *phiP, const double *P, int n, int m, int r,
+                                                  uint32_t gr, double *B, const double *X, float *R32, int e0,
+                                                  bool store_r, int lane)
 {
     const int tot = n * r;
     int ee[NE], ii[NE], qq[NE], off[NE];
@@ -654,16 +648,17 @@ __device__ __forceinline__ void split_at(const double *a, int ad, float &hi, flo
 // a double-float sum and subtracted from r_old, itself a double-float pair.  The error of
 // A d is ~2^-44 |A||d| with |d| ~ 1e-5 |x|, and the pair holds r_old to 2^-47 of its size
 // (~1e-5 |A||x|), both far below FP64 rounding of |A||x|, so the refinement converges as with
-// an FP64 residual.  B holds r_old as (hi, lo) pairs and receives r_new; R32 receives hi.  Phi rows lane-per-row (the split of Phi_ij shared by the row's
-// operators), P' rows lane-per-element.  PRE: Phi and P hold their splits already.
+// an FP64 residual.  B holds r_old as (hi, lo) pairs and receives r_new; R32 receives hi.
+// Phi rows lane-per-row (the split of Phi_ij shared by the row's operators, two operators per
+// packed instruction), P' rows lane-per-element.  PRE: Phi and P hold their splits already.
 template <int SP, int SM, int RMAX, bool PRE>
-__device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, uint32_t gr, double *B,
-                                            float *R32, int lane)
+__device__ __forceinline__ void residual_df(const double *phiP, const double *P, int n, int m, int r, uint32_t gr,
+                                            double *B, float *R32, int lane)
 {
     constexpr int NS = RegRows<SP>::NS;
     float sh[NS][RMAX], sl[NS][RMAX];
-#if RBFFD_DF_PACKED
-    // Phi and P rows: the operators' sums in pairs (q, q + 1); a pair past r computes on zeros
+    // Phi and P rows: the operators' sums in pairs (q, q + 1), packed FP32; a pair past r
+    // computes on zeros
     constexpr int QP = (RMAX + 1) / 2;
 #pragma unroll
     for (int k = 0; k < NS; k++) {
@@ -708,46 +703,6 @@ __device__ __forceinline__ void residual_df(const double *phiP, const double *P,
             }
         }
     }
-#else
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-#pragma unroll
-        for (int q = 0; q < RMAX; q++) sh[k][q] = sl[k][q] = 0.0f;
-        if (32 * k >= n) continue;
-        const int i = lane + 32 * k;
-        const int ii = i < n ? i : n - 1;
-        const int offi = tri_off(ii);
-        int offj = 0;
-        for (int jj = 0; jj < n; jj++) {
-            const int ad = jj <= ii ? offi + jj : offj + ii;
-            offj += jj + 1;
-            float ah, al;
-            split_at<PRE>(phiP, ad, ah, al);
-            const float *dj = R32 + jj * r;
-#pragma unroll
-            for (int q = 0; q < RMAX; q++) {
-                if (q < r) {
-                    const float d = dj[q];
-                    df_mac(ah, d, sh[k][q], sl[k][q]);
-                    sl[k][q] = fmaf(al, d, sl[k][q]);
-                }
-            }
-        }
-        for (int l = 0; l < m; l++) {
-            float ah, al;
-            split_at<PRE>(P, ii * m + l, ah, al);
-            const float *dl = R32 + (n + l) * r;
-#pragma unroll
-            for (int q = 0; q < RMAX; q++) {
-                if (q < r) {
-                    const float d = dl[q];
-                    df_mac(ah, d, sh[k][q], sl[k][q]);
-                    sl[k][q] = fmaf(al, d, sl[k][q]);
-                }
-            }
-        }
-    }
-#endif
     constexpr int PE = (SM * RMAX + 31) / 32;  // P' elements per lane (m r <= SM RMAX)
     float th[PE], tl[PE];
 #pragma unroll
@@ -1130,7 +1085,9 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
         RegRows<SP> RP;
         fill_phi_rows<SP>(RP, x32, n, p, lane);
         bool ok = reg_gj<SP>(RP, n, permP, dinvP, prow, lane);
-        if (ok) ok = build_schur<SP, SM>(RP, n, m, div19_magic(m), permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS, prow, lane);
+        if (ok)
+            ok = build_schur<SP, SM>(RP, n, m, div19_magic(m), permP, P32, Pp, G, ldg, Sm, Sinv, lds, permS, dinvS,
+                                     prow, lane);
         bool fallback = !ok;
         if (ok) assemble_phi_packed(xs, n, m, deg, p, phiP, P, xf, lane);
         int64_t r0, r1;
