@@ -1799,24 +1799,23 @@ struct EarlyCsc : PatternHook {
         active = true;
         CK(cudaMemsetAsync(count, 0, sizeof(int64_t) * (N + 1), st));
         CK(cudaMemsetAsync(fill, 0, sizeof(int64_t) * N, st));
+        if (nchunk > 0 && (nchunk > RBFFD_MAX_CHUNKS || nnz > INT32_MAX || N < (int64_t)nchunk * 1024)) nchunk = 0;
+        if (nchunk > 0) CK(cudaMallocAsync((void **)&inv, sizeof(int32_t) * nnz, st));
         CK(launch_csc_count(nnz, nbr, count, st));
         CK(scan_exclusive_i64(count, colstart, N, scratch, tb, st));
-        CK(launch_csc_scatter(N, row_ptr, nbr, 0, colstart, fill, rowval, perm, st));
-        CK(launch_csc_sort_segments(N, colstart, rowval, perm, N, st));
+        // rows 1-based as scattered (Julia's rowval); the sort writes the inverse permutation
+        CK(launch_csc_scatter(N, row_ptr, nbr, 1, colstart, fill, rowval, perm, st));
+        CK(launch_csc_sort_segments(N, colstart, rowval, perm, N + 1, st, inv));
         CK(launch_add_i64(N + 1, colstart, 1, st));  // Julia is 1-based
-        CK(launch_add_i64(nnz, rowval, 1, st));
         CK(cudaFreeAsync(count, st));
         CK(cudaFreeAsync(fill, st));
         CK(cudaFreeAsync(scratch, st));
         CK(cudaEventRecord(h->side_ev[0], st));
-        if (nchunk > 0 && (nchunk > RBFFD_MAX_CHUNKS || nnz > INT32_MAX || N < (int64_t)nchunk * 1024)) nchunk = 0;
         if (nchunk > 0) {
             int *cm;
             int64_t *cp;
-            CK(cudaMallocAsync((void **)&inv, sizeof(int32_t) * nnz, st));
             CK(cudaMallocAsync((void **)&cm, sizeof(int) * nchunk, st));
             CK(cudaMallocAsync((void **)&cp, sizeof(int64_t) * nchunk, st));
-            CK(launch_invert_perm(nnz, perm, inv, st));
             CK(launch_chunk_bounds(N, n, nbr, nchunk, colstart, cm, cp, st));
             CK(cudaMemcpyAsync(hcp, cp, sizeof(int64_t) * nchunk, cudaMemcpyDeviceToHost, st));
             CK(cudaFreeAsync(cm, st));

@@ -248,14 +248,13 @@ cudaError_t launch_csc_count(int64_t nnz, const int32_t *col, int64_t *colcount,
 cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32_t *col,
                                int64_t row_begin, const int64_t *colstart, int64_t *fill,
                                int64_t *rowval, int64_t *perm, cudaStream_t st);
-// Sorts each column segment of (rowval, perm) by row; row_limit bounds the row ids (0-based).
+// Sorts each column segment of (rowval, perm) by row; row_limit bounds the row ids.  With inv
+// non-null it also writes the inverse permutation inv[perm[p]] = p (int32 positions).
 cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                     int64_t *perm, int64_t row_limit, cudaStream_t st);
+                                     int64_t *perm, int64_t row_limit, cudaStream_t st, int32_t *inv = nullptr);
 cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *src, double *dst,
                               cudaStream_t st);
 cudaError_t launch_add_i64(int64_t n, int64_t *a, int64_t v, cudaStream_t st);
-// inv[perm[k]] = k (the CSR -> CSC position map of an export).
-cudaError_t launch_invert_perm(int64_t nnz, const int64_t *perm, int32_t *inv, cudaStream_t st);
 // Collocated uniform stencils (row r = node r, nbr N x n) solved in C chunks of consecutive
 // rows: cp[i] = the number of leading CSC entries (columns referenced only by rows of chunks
 // <= i) that are final once chunks 0..i are solved; colstart1 = the 1-based CSC column starts;

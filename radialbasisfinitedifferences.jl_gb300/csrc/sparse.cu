@@ -695,7 +695,8 @@ __global__ void csc_count_kernel(int64_t nnz, const int32_t *col, unsigned long 
         atomicAdd(&cnt[col[t]], 1ull);
 }
 
-// Scatter every CSR entry to its column; rowval gets the 0-based row id, perm the CSR position.
+// Scatter every CSR entry to its column; rowval gets the row id plus row_begin (a row offset,
+// or 1 for 1-based rows), perm the CSR position.
 __global__ void csc_scatter_kernel(int64_t rows, const int64_t *row_ptr, const int32_t *col,
                                    int64_t row_begin, const int64_t *colstart,
                                    unsigned long long *fill, int64_t *rowval, int64_t *perm)
@@ -716,8 +717,10 @@ __global__ void csc_scatter_kernel(int64_t rows, const int64_t *row_ptr, const i
 // Sort each column segment by row.  Warp per column: rank of each entry = number of entries
 // with a smaller row (rows inside a column are distinct); segments longer than 256 fall back
 // to one lane's insertion sort.
+// With inv non-null, also inv[perm[p]] = p for every final position p (the inverse of the
+// gather permutation: CSR position -> CSC position).
 __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                int64_t *perm, bool keys32)
+                                int64_t *perm, bool keys32, int32_t *inv)
 {
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -725,7 +728,10 @@ __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t 
     for (int64_t c = warp; c < ncols; c += nw) {
         int64_t a = colstart[c], b = colstart[c + 1];
         int len = (int)(b - a);
-        if (len <= 1) continue;
+        if (len <= 1) {
+            if (inv && len == 1 && lane == 0) inv[perm[a]] = (int32_t)a;
+            continue;
+        }
         if (keys32 && len <= 64) {
             // The common case (a column of a kNN operator holds ~k rows): rank sort of two
             // register slots with 32-bit keys.  Row ids within a column are distinct, and the
@@ -753,10 +759,12 @@ __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t 
             if (lane < len) {
                 rowval[a + rk0] = r0;
                 perm[a + rk0] = p0;
+                if (inv) inv[p0] = (int32_t)(a + rk0);
             }
             if (t1 < len) {
                 rowval[a + rk1] = r1;
                 perm[a + rk1] = p1;
+                if (inv) inv[p1] = (int32_t)(a + rk1);
             }
         } else if (len <= 256) {
             int64_t rv[8], pv[8];
@@ -787,6 +795,7 @@ __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t 
                 if (t < len) {
                     rowval[a + rk[k]] = rv[k];
                     perm[a + rk[k]] = pv[k];
+                    if (inv) inv[pv[k]] = (int32_t)(a + rk[k]);
                 }
             }
         } else if (lane == 0) {
@@ -801,6 +810,8 @@ __global__ void csc_sort_kernel(int64_t ncols, const int64_t *colstart, int64_t 
                 rowval[j + 1] = rvi;
                 perm[j + 1] = pvi;
             }
+            if (inv)
+                for (int64_t i = a; i < b; i++) inv[perm[i]] = (int32_t)i;
         }
         __syncwarp();
     }
@@ -811,13 +822,6 @@ __global__ void gather_f64_kernel(int64_t n, const int64_t *perm, const double *
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x)
         dst[t] = src[perm[t]];
-}
-
-__global__ void invert_perm_kernel(int64_t n, const int64_t *perm, int32_t *inv)
-{
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-         t += (int64_t)gridDim.x * blockDim.x)
-        inv[perm[t]] = (int32_t)t;
 }
 
 // cm[k] = min over the rows of chunk k (rows [k N / C, (k + 1) N / C)) of the smallest column
@@ -1088,10 +1092,10 @@ cudaError_t launch_csc_scatter(int64_t rows, const int64_t *row_ptr, const int32
 }
 
 cudaError_t launch_csc_sort_segments(int64_t ncols, const int64_t *colstart, int64_t *rowval,
-                                     int64_t *perm, int64_t row_limit, cudaStream_t st)
+                                     int64_t *perm, int64_t row_limit, cudaStream_t st, int32_t *inv)
 {
     const bool keys32 = row_limit < 0xffffffffll;  // row ids fit 32-bit keys below the padding key
-    csc_sort_kernel<<<blocks_for(ncols * 32, 256), 256, 0, st>>>(ncols, colstart, rowval, perm, keys32);
+    csc_sort_kernel<<<blocks_for(ncols * 32, 256), 256, 0, st>>>(ncols, colstart, rowval, perm, keys32, inv);
     return cudaGetLastError();
 }
 
@@ -1099,12 +1103,6 @@ cudaError_t launch_gather_f64(int64_t nnz, const int64_t *perm, const double *sr
                               cudaStream_t st)
 {
     gather_f64_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, perm, src, dst);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_invert_perm(int64_t nnz, const int64_t *perm, int32_t *inv, cudaStream_t st)
-{
-    invert_perm_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, perm, inv);
     return cudaGetLastError();
 }
 
