@@ -186,6 +186,20 @@ int rbffd_calculateneighbors(rbffd_handle *h, const double *X, int64_t N, const 
                              int64_t M, int n, const int32_t *node_class, int64_t *idxs_x,
                              double *dists_x, int64_t *idxs_y_x, double *dists_y_x);
 
+/* processmesh(meshname, markernames) -- src/processmesh.jl:1-192 -- after its HDF5/CGNS
+   reads (extractcoordinates.jl, extractelements.jl), which stay with the caller.
+   vertices: nv points (x, y) (Base/dom-1/GridCoordinates); tri: 3 ntri 1-based vertex ids
+   (TriElements/ElementConnectivity); bc: 2 nbc 1-based vertex ids, the line elements of
+   every marker concatenated in element-range order.  Y receives ntri + 2 nbc points: the
+   triangle centroids, the line midpoints, then the ghost nodes; normals / tangents (nbc x 2)
+   the lines' unit normals [-dy, dx]/|.| and tangents, oriented by the sign of
+   dot(first midpoint - its nearest centroid, first normal); *offset the mean distance of
+   the midpoints to their nearest centroid (ghost = midpoint + normal * offset).  The nearest
+   centroid is exact (the reference's HNSW search is approximate).  Host pointers. */
+int rbffd_process_mesh(rbffd_handle *h, const double *vertices, int64_t nv, const int64_t *tri,
+                       int64_t ntri, const int64_t *bc, int64_t nbc, double *Y, double *normals,
+                       double *tangents, double *offset);
+
 /* ---------------------------------------------------------------------------------
  * Device-resident operator sets (time stepping, benchmarks).
  * ------------------------------------------------------------------------------ */

@@ -51,6 +51,7 @@ def lib():
         L.orc_spmv_csc.restype = None
         L.orc_phi.argtypes = [i32, i32, i32, ctypes.c_double, ctypes.c_double]
         L.orc_phi.restype = ctypes.c_double
+        L.orc_process_mesh.argtypes = [P, i64, P, i64, P, i64, P, P, P, P]
         L.orc_max_threads.restype = i32
         global _all_threads
         _all_threads = L.orc_max_threads()
@@ -181,3 +182,20 @@ def spmv_csc(M, colptr, rowval, nzval, x):
 
 def phi(p, a, b, x, y):
     return lib().orc_phi(p, a, b, float(x), float(y))
+
+
+def process_mesh(V, tri, bc):
+    """processmesh after the file reads (oracle/rbffd_oracle.c orc_process_mesh): V (nv, 2)
+    vertices, tri (ntri, 3) and bc (nbc, 2) 1-based vertex ids.  Returns (Y, normals,
+    tangents, offset): Y stacks the centroids, the boundary midpoints and the ghost nodes."""
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    tri = np.ascontiguousarray(tri, dtype=np.int64)
+    bc = np.ascontiguousarray(bc, dtype=np.int64)
+    ntri, nbc = len(tri), len(bc)
+    Y = np.empty((ntri + 2 * nbc, 2))
+    nrm, tng = np.empty((nbc, 2)), np.empty((nbc, 2))
+    off = ctypes.c_double()
+    rc = lib().orc_process_mesh(_p(V), len(V), _p(tri), ntri, _p(bc), nbc, _p(Y), _p(nrm), _p(tng), ctypes.byref(off))
+    if rc:
+        raise OracleError(rc, "orc_process_mesh")
+    return Y, nrm, tng, off.value

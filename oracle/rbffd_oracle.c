@@ -34,6 +34,12 @@
  *       followed by an explicit inverse, then M_inv * RHS as the reference does.
  *   SparseArrays sparse(I,J,V): restated as a counting sort into 1-based CSC that keeps
  *       explicit zeros.
+ *   HNSW.jl 0.1 HierarchicalNSW + knn_search (processmesh's nearest interior node): an
+ *       approximate nearest-neighbour graph search; restated as the exact nearest node
+ *       (the two agree whenever the graph search finds the true neighbour).
+ *   Statistics mean of a Vector{Float64}: a sum in index order divided by the length
+ *       (Julia's own summation order is blocked and SIMD-reassociated, so the last bit of
+ *       the mean may differ).
  */
 #include <math.h>
 #include <stdint.h>
@@ -804,4 +810,78 @@ void orc_spmv_csc(int64_t M, int64_t N, const int64_t *colptr, const int64_t *ro
         double xj = x[j];
         for (int64_t t = colptr[j] - 1; t < colptr[j + 1] - 1; t++) y[rowval[t] - 1] += nzval[t] * xj;
     }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Mesh ingest: processmesh after its file reads.                            */
+/* ------------------------------------------------------------------------- */
+
+/* processmesh (src/processmesh.jl:1-192) on arrays already read from the CGNS file:
+     V    nv vertices (x, y)                       extractcoordinates.jl:1-14
+     tri  3 ntri 1-based vertex ids of the triangles (TriElements/ElementConnectivity)
+     bc   2 nbc 1-based vertex ids of the boundary line elements of every marker,
+          concatenated in element-range order (each marker's ElementConnectivity)
+   Outputs:
+     Y    (ntri + 2 nbc) points: the triangles' centroids (extractelements.jl:16-17,
+          processmesh.jl:23-27), the lines' midpoints (processmesh.jl:89, 116), then the
+          ghost nodes (processmesh.jl:167-181, genghostnodes.jl:1-6)
+     nrm, tng  nbc unit normals [-dy, dx] / |.| and tangents [dx, dy] / |.| of the lines
+          (calculatenormal.jl:1-17), all multiplied by the sign of
+          dot(line 1 midpoint - its nearest centroid, normal 1) (processmesh.jl:120-133)
+     offset  the mean distance of the midpoints to their nearest centroid
+          (processmesh.jl:135-165); ghost = midpoint + normal * offset.
+   Returns ORC_EINVAL on an empty mesh or a vertex id out of range. */
+int orc_process_mesh(const double *V, int64_t nv, const int64_t *tri, int64_t ntri, const int64_t *bc,
+                     int64_t nbc, double *Y, double *nrm, double *tng, double *offset)
+{
+    if (nv <= 0 || ntri <= 0 || nbc <= 0) return ORC_EINVAL;
+    for (int64_t t = 0; t < 3 * ntri; t++)
+        if (tri[t] < 1 || tri[t] > nv) return ORC_EINVAL;
+    for (int64_t t = 0; t < 2 * nbc; t++)
+        if (bc[t] < 1 || bc[t] > nv) return ORC_EINVAL;
+    for (int64_t e = 0; e < ntri; e++) {
+        const double *a = V + 2 * (tri[3 * e] - 1), *b = V + 2 * (tri[3 * e + 1] - 1), *c = V + 2 * (tri[3 * e + 2] - 1);
+        Y[2 * e] = (a[0] + b[0] + c[0]) / 3.0; /* mean of three SVectors: ((a + b) + c) / 3 */
+        Y[2 * e + 1] = (a[1] + b[1] + c[1]) / 3.0;
+    }
+    double *M = Y + 2 * ntri, *G = Y + 2 * (ntri + nbc);
+    for (int64_t e = 0; e < nbc; e++) {
+        const double *a = V + 2 * (bc[2 * e] - 1), *b = V + 2 * (bc[2 * e + 1] - 1);
+        M[2 * e] = (a[0] + b[0]) / 2.0;
+        M[2 * e + 1] = (a[1] + b[1]) / 2.0;
+        const double dx = b[0] - a[0], dy = b[1] - a[1];
+        const double len = sqrt(dy * dy + dx * dx); /* norm([-dy, dx]) */
+        nrm[2 * e] = -dy / len;
+        nrm[2 * e + 1] = dx / len;
+        tng[2 * e] = dx / len;
+        tng[2 * e + 1] = dy / len;
+    }
+    int32_t *nn = (int32_t *)malloc(sizeof(int32_t) * (size_t)nbc);
+    double *d2 = (double *)malloc(sizeof(double) * (size_t)nbc);
+    if (!nn || !d2) {
+        free(nn);
+        free(d2);
+        return ORC_ENOMEM;
+    }
+    int rc = orc_knn(Y, ntri, M, nbc, 1, NULL, NULL, nn, d2, 1);
+    if (rc) {
+        free(nn);
+        free(d2);
+        return rc;
+    }
+    const double *c0 = Y + 2 * (int64_t)nn[0];
+    const double dt = (M[0] - c0[0]) * nrm[0] + (M[1] - c0[1]) * nrm[1];
+    const double sg = dt > 0.0 ? 1.0 : (dt < 0.0 ? -1.0 : dt); /* Julia sign */
+    double sum = 0.0;
+    for (int64_t e = 0; e < nbc; e++) sum += sqrt(d2[e]);
+    const double off = fabs(sum / (double)nbc);
+    for (int64_t e = 0; e < 2 * nbc; e++) {
+        nrm[e] = sg * nrm[e];
+        tng[e] = sg * tng[e];
+        G[e] = M[e] + nrm[e] * off;
+    }
+    *offset = off;
+    free(nn);
+    free(d2);
+    return ORC_OK;
 }

@@ -19,6 +19,7 @@ from .operators import (  # noqa: F401
     generate_operator,
     hyperviscosity_operator,
     node_class_from_ranges,
+    processmesh_arrays,
 )
 
 

@@ -28,6 +28,7 @@ EXPORTED = [
     "rbffd_hyperviscosity_operator",
     "rbffd_generate_operator_unscaled",
     "rbffd_calculateneighbors",
+    "rbffd_process_mesh",
     "rbffd_opset_create",
     "rbffd_opset_destroy",
     "rbffd_opset_shape",
@@ -157,6 +158,7 @@ def load(build_if_missing=False):
         "rbffd_hyperviscosity_operator": ([P, i32, P, i64, P, i64, i32, i32, i32, P, i32, P, P], i32),
         "rbffd_generate_operator_unscaled": ([P, P, i64, i32, i32, i32, u32, i32, P, P], i32),
         "rbffd_calculateneighbors": ([P, P, i64, P, i64, i32, P, P, P, P, P], i32),
+        "rbffd_process_mesh": ([P, P, i64, P, i64, P, i64, P, P, P, P], i32),
         "rbffd_opset_create": ([P, P, P, P], i32),
         "rbffd_opset_destroy": ([P, P], None),
         "rbffd_opset_shape": ([P, P, P, P, P], i32),

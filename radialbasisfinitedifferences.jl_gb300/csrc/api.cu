@@ -291,6 +291,78 @@ __global__ void knn_export(const int32_t *idx, const double *d2, int64_t n, int6
     }
 }
 
+// processmesh after its file reads (src/processmesh.jl): triangle centroids, mean of three
+// vertices summed in order then divided (extractelements.jl:16-17).  Vertex ids are 1-based;
+// an id out of range sets *bad.
+__global__ void mesh_centroids(const double2 *V, int64_t nv, const int64_t *tri, int64_t ntri, double2 *C, int *bad)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ntri; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = tri[3 * e] - 1, b = tri[3 * e + 1] - 1, c = tri[3 * e + 2] - 1;
+        if (a < 0 || a >= nv || b < 0 || b >= nv || c < 0 || c >= nv) {
+            atomicExch(bad, 1);
+            C[e] = make_double2(0.0, 0.0);
+            continue;
+        }
+        const double2 pa = V[a], pb = V[b], pc = V[c];
+        C[e] = make_double2(__ddiv_rn(__dadd_rn(__dadd_rn(pa.x, pb.x), pc.x), 3.0),
+                            __ddiv_rn(__dadd_rn(__dadd_rn(pa.y, pb.y), pc.y), 3.0));
+    }
+}
+
+// Boundary line elements: midpoints, and the unit normal [-dy, dx] / |.| and tangent
+// [dx, dy] / |.| of calculatenormal (src/calculatenormal.jl:1-17), with |.| =
+// sqrt(dy^2 + dx^2) in that order, every operation rounded once.
+__global__ void mesh_lines(const double2 *V, int64_t nv, const int64_t *bc, int64_t nbc, double2 *M, double2 *Nrm,
+                           double2 *Tng, int *bad)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nbc; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = bc[2 * e] - 1, b = bc[2 * e + 1] - 1;
+        if (a < 0 || a >= nv || b < 0 || b >= nv) {
+            atomicExch(bad, 1);
+            M[e] = Nrm[e] = Tng[e] = make_double2(0.0, 0.0);
+            continue;
+        }
+        const double2 pa = V[a], pb = V[b];
+        M[e] = make_double2(__ddiv_rn(__dadd_rn(pa.x, pb.x), 2.0), __ddiv_rn(__dadd_rn(pa.y, pb.y), 2.0));
+        const double dx = __dsub_rn(pb.x, pa.x), dy = __dsub_rn(pb.y, pa.y);
+        const double len = __dsqrt_rn(__dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx)));
+        Nrm[e] = make_double2(__ddiv_rn(-dy, len), __ddiv_rn(dx, len));
+        Tng[e] = make_double2(__ddiv_rn(dx, len), __ddiv_rn(dy, len));
+    }
+}
+
+// One CTA: the ghost offset (the mean distance of the midpoints to their nearest centroid,
+// per-thread sums over contiguous ranges then a fixed tree: a deterministic order), the
+// orientation sign from the first line (processmesh.jl:120-133), and the ghost nodes
+// midpoint + normal * offset (genghostnodes.jl:1-6).  Needs blockDim.x == 256.
+__global__ void mesh_ghosts(const double2 *C, const double2 *M, const int32_t *nn, const double *d2, int64_t nbc,
+                            double2 *Nrm, double2 *Tng, double2 *G, double *offset)
+{
+    __shared__ double part[256];
+    const int t = threadIdx.x;
+    const int64_t chunk = (nbc + 255) / 256, e0 = t * chunk, e1 = e0 + chunk < nbc ? e0 + chunk : nbc;
+    double s = 0.0;
+    for (int64_t e = e0; e < e1; e++) s = __dadd_rn(s, __dsqrt_rn(d2[e]));
+    part[t] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) part[t] = __dadd_rn(part[t], part[t + w]);
+        __syncthreads();
+    }
+    const double off = fabs(__ddiv_rn(part[0], (double)nbc));
+    const double2 m0 = M[0], c0 = C[nn[0]], n0 = Nrm[0];
+    const double dt = __dadd_rn(__dmul_rn(__dsub_rn(m0.x, c0.x), n0.x), __dmul_rn(__dsub_rn(m0.y, c0.y), n0.y));
+    const double sg = dt > 0.0 ? 1.0 : (dt < 0.0 ? -1.0 : dt);  // Julia's sign
+    __syncthreads();  // every thread has read the first normal
+    for (int64_t e = t; e < nbc; e += blockDim.x) {
+        const double2 nv = make_double2(__dmul_rn(sg, Nrm[e].x), __dmul_rn(sg, Nrm[e].y));
+        Nrm[e] = nv;
+        Tng[e] = make_double2(__dmul_rn(sg, Tng[e].x), __dmul_rn(sg, Tng[e].y));
+        G[e] = make_double2(__dadd_rn(M[e].x, __dmul_rn(nv.x, off)), __dadd_rn(M[e].y, __dmul_rn(nv.y, off)));
+    }
+    if (t == 0) *offset = off;
+}
+
 int nblk(int64_t n, int t = 256)
 {
     int64_t b = (n + t - 1) / t;
@@ -2002,6 +2074,61 @@ RBFFD_EXPORT int rbffd_generate_operator_unscaled(rbffd_handle *h, const double 
     rc = export_all(h, s, out);
     rbffd_opset_destroy(h, s);
     return rc;
+}
+
+RBFFD_EXPORT int rbffd_process_mesh(rbffd_handle *h, const double *vertices, int64_t nv, const int64_t *tri,
+                                    int64_t ntri, const int64_t *bc, int64_t nbc, double *Y, double *normals,
+                                    double *tangents, double *offset)
+{
+    if (!h) return RBFFD_EINVAL;
+    if (!vertices || nv <= 0 || !tri || ntri <= 0 || ntri > INT32_MAX || !bc || nbc <= 0 || !Y || !normals ||
+        !tangents || !offset)
+        return fail(h, RBFFD_EINVAL, "bad process_mesh arguments");
+    cudaSetDevice(h->device);
+    cudaStream_t st = h->stream;
+    Arena tmp(st);
+    double2 *dV, *dY, *dN, *dT;
+    int64_t *dtri, *dbc;
+    int *bad;
+    CK(stage(h, tmp, vertices, (size_t)nv, RBFFD_MEM_HOST, &dV));
+    CK(stage(h, tmp, tri, (size_t)(3 * ntri), RBFFD_MEM_HOST, &dtri));
+    CK(stage(h, tmp, bc, (size_t)(2 * nbc), RBFFD_MEM_HOST, &dbc));
+    CK(tmp.get(&dY, ntri + 2 * nbc));
+    CK(tmp.get(&dN, nbc));
+    CK(tmp.get(&dT, nbc));
+    CK(tmp.zeros(&bad, 1));
+    double2 *C = dY, *M = dY + ntri, *G = dY + ntri + nbc;
+    mesh_centroids<<<nblk(ntri), 256, 0, st>>>(dV, nv, dtri, ntri, C, bad);
+    mesh_lines<<<nblk(nbc), 256, 0, st>>>(dV, nv, dbc, nbc, M, dN, dT, bad);
+    CK(cudaGetLastError());
+    int hbad = 0;
+    CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hbad) return fail(h, RBFFD_EINVAL, "process_mesh: vertex id out of range");
+    // the nearest centroid of every midpoint (processmesh.jl:120-127, 135-160), exact
+    GridBuild gb;
+    int rc = build_grid(h, tmp, C, nullptr, ntri, gb);
+    if (rc) return rc;
+    int32_t *nn;
+    double *d2, *doff;
+    int *err;
+    CK(tmp.get(&nn, nbc));
+    CK(tmp.get(&d2, nbc));
+    CK(tmp.get(&doff, 1));
+    CK(tmp.zeros(&err, 1));
+    CK(launch_knn(gb.g, M, nullptr, nullptr, false, nbc, nullptr, 1, 1, nullptr, nn, d2, knn_r0(gb.rho, 1), err,
+                  h->num_sms, st));
+    mesh_ghosts<<<1, 256, 0, st>>>(C, M, nn, d2, nbc, dN, dT, G, doff);
+    CK(cudaGetLastError());
+    int herr = 0;
+    CK(cudaMemcpyAsync(Y, dY, sizeof(double2) * (size_t)(ntri + 2 * nbc), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(normals, dN, sizeof(double2) * (size_t)nbc, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(tangents, dT, sizeof(double2) * (size_t)nbc, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(offset, doff, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (herr) return fail(h, RBFFD_EINVAL, "process_mesh: nearest-centroid search failed");
+    return RBFFD_OK;
 }
 
 RBFFD_EXPORT int rbffd_calculateneighbors(rbffd_handle *h, const double *X, int64_t N, const double *Y,

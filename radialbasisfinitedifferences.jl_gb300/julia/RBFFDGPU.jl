@@ -215,6 +215,43 @@ function calculateneighbors(X, Y, n, X_idx_in, X_idx_bc, X_idx_bc_g, Y_idx_in, Y
     return idxs_x, idxs_y_x, dists_x, dists_y_x
 end
 
+# processmesh(meshname, markernames) (src/processmesh.jl:1-192) after its HDF5/CGNS reads,
+# which stay in Julia (HDF5.jl): vertices from Base/dom-1/GridCoordinates, the triangles'
+# and every marker's ElementConnectivity.  Returns the reference's Y, Y_idx_in, Y_idx_bc,
+# Y_idx_bc_g, bc_normals and bc_tangents (the VTK cells are the caller's), plus the ghost
+# offset.
+function processmesh_arrays(vertices, tri_conn::AbstractMatrix{<:Integer},
+                            bc_conns::AbstractVector{<:AbstractMatrix{<:Integer}}; h = handle())
+    V = points(vertices)
+    T = Matrix{Int64}(tri_conn)                        # 3 x ntri, 1-based (CGNS order)
+    B = reduce(hcat, [Matrix{Int64}(b) for b in bc_conns])  # 2 x nbc, markers in element-range order
+    ntri, nbc = size(T, 2), size(B, 2)
+    Y = Vector{SVector{2,Float64}}(undef, ntri + 2nbc)
+    nrm = Vector{SVector{2,Float64}}(undef, nbc)
+    tng = Vector{SVector{2,Float64}}(undef, nbc)
+    off = Ref{Float64}(0.0)
+    GC.@preserve V T B Y nrm tng begin
+        rc = ccall((:rbffd_process_mesh, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Int64}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Float64},
+             Ptr{Float64}, Ref{Float64}),
+            h.ptr, pointer(reinterpret(Float64, V)), length(V), pointer(T), ntri, pointer(B), nbc,
+            pointer(reinterpret(Float64, Y)), pointer(reinterpret(Float64, nrm)), pointer(reinterpret(Float64, tng)),
+            off)
+    end
+    check(h, rc, Ref(Stats()))
+    Y_idx_bc, Y_idx_bc_g, bc_normals, bc_tangents = UnitRange{Int}[], UnitRange{Int}[], [], []
+    a = 0
+    for b in bc_conns
+        m = size(b, 2)
+        push!(Y_idx_bc, (ntri + a + 1):(ntri + a + m))
+        push!(Y_idx_bc_g, (ntri + nbc + a + 1):(ntri + nbc + a + m))
+        push!(bc_normals, nrm[(a + 1):(a + m)])
+        push!(bc_tangents, tng[(a + 1):(a + m)])
+        a += m
+    end
+    return Y, 1:ntri, Y_idx_bc, Y_idx_bc_g, bc_normals, bc_tangents, off[]
+end
+
 # ----------------------------------------------------------------------------------------
 # Device-resident operators and time stepping (examples/adv_diff_test.jl:144-199).  Field
 # arguments are device buffers: any object whose `pointer` is a device address (a CUDA.jl
@@ -350,7 +387,7 @@ function SparseArrays.SparseMatrixCSC(A::DeviceOperator)
     return SparseMatrixCSC(rows, cols, colptr, rowval, nzval)
 end
 
-export generate_operator, hyperviscosity_operator, calculateneighbors, OperatorSet, spmv!, RK4, step!,
+export generate_operator, hyperviscosity_operator, calculateneighbors, processmesh_arrays, OperatorSet, spmv!, RK4, step!,
        DeviceOperator
 
 end # module

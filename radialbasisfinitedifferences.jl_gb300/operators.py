@@ -226,6 +226,36 @@ def calculateneighbors(X, Y, n, X_idx_in=None, X_idx_bc=(), X_idx_bc_g=(), Y_idx
     return ix, iy, dx, dy
 
 
+def processmesh_arrays(vertices, tri, bc_lines, handle=None):
+    """processmesh(meshname, markernames) (src/processmesh.jl:1-192) after its HDF5/CGNS
+    reads, on arrays: vertices (nv, 2); tri (ntri, 3) 1-based vertex ids of the triangles;
+    bc_lines: one (nb_i, 2) array of 1-based vertex ids per marker, in element-range order.
+    Returns (Y, Y_idx_in, Y_idx_bc, Y_idx_bc_g, bc_normals, bc_tangents, offset) as the
+    reference does (1-based index ranges as Python ranges, per-marker normal and tangent
+    arrays), with Y the centroids, the line midpoints and the ghost nodes."""
+    h = handle or default_handle()
+    L = nat.load()
+    V = _pts(vertices)
+    T = np.ascontiguousarray(tri, dtype=np.int64).reshape(-1, 3)
+    parts = [np.ascontiguousarray(b, dtype=np.int64).reshape(-1, 2) for b in bc_lines]
+    B = np.ascontiguousarray(np.concatenate(parts)) if parts else np.empty((0, 2), np.int64)
+    ntri, nbc = len(T), len(B)
+    Y = np.empty((ntri + 2 * nbc, 2))
+    nrm, tng = np.empty((nbc, 2)), np.empty((nbc, 2))
+    off = ctypes.c_double()
+    rc = L.rbffd_process_mesh(h.ptr, _ptr(V), len(V), _ptr(T), ntri, _ptr(B), nbc, _ptr(Y), _ptr(nrm), _ptr(tng),
+                              ctypes.byref(off))
+    nat.check(h.ptr, rc)
+    idx_bc, idx_g, normals, tangents, a = [], [], [], [], 0
+    for p in parts:
+        idx_bc.append(range(ntri + a + 1, ntri + a + len(p) + 1))
+        idx_g.append(range(ntri + nbc + a + 1, ntri + nbc + a + len(p) + 1))
+        normals.append(nrm[a:a + len(p)])
+        tangents.append(tng[a:a + len(p)])
+        a += len(p)
+    return Y, range(1, ntri + 1), idx_bc, idx_g, normals, tangents, off.value
+
+
 class GhostClosure:
     """Ghost-node closure of one boundary (rbffd_ghost_*): u[G] = -inv(A[B,G]) A[B,~G] u with A
     one operator of a collocated set, B the boundary nodes and G their ghosts

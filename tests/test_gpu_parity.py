@@ -572,3 +572,34 @@ def test_rk4_matches_reference_integration(pkg, orc, gpu, dtype, tol, F):
             st.apply(torch.tensor(U0, dtype=td, device="cuda"), y)
             LU = L @ U0
             assert np.abs(y.double().cpu().numpy() - LU).max() <= max(tol, 1e-12) * 10 * np.abs(LU).max()
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+@pytest.mark.parametrize("nx,ny", [(12, 9), (160, 120)])
+def test_process_mesh_matches_oracle(pkg, orc, gpu, reverse, nx, ny):
+    """processmesh after its file reads (src/processmesh.jl:1-192) through the C ABI:
+    centroids, midpoints, normals and tangents bit-exact with the oracle, the offset and the
+    ghost nodes to rounding (the mean is summed in another order), index ranges as the
+    reference builds them."""
+    from conftest import rect_tri_mesh
+
+    V, tri, markers = rect_tri_mesh(nx, ny, seed=4, reverse=reverse)
+    Y, idx_in, idx_bc, idx_g, normals, tangents, off = pkg.processmesh_arrays(V, tri, markers)
+    Yr, nr, tr, offr = orc.process_mesh(V, tri, np.concatenate(markers))
+    ntri, nbc = len(tri), sum(len(m) for m in markers)
+    assert np.array_equal(Y[:ntri + nbc], Yr[:ntri + nbc])
+    assert np.array_equal(np.concatenate(normals), nr) and np.array_equal(np.concatenate(tangents), tr)
+    assert off == pytest.approx(offr, rel=1e-13)
+    assert np.allclose(Y[ntri + nbc:], Yr[ntri + nbc:], rtol=0, atol=1e-15)
+    assert idx_in == range(1, ntri + 1)
+    assert [len(r) for r in idx_bc] == [len(m) for m in markers] == [len(r) for r in idx_g]
+    assert idx_bc[0].start == ntri + 1 and idx_g[-1].stop == ntri + 2 * nbc + 1
+
+
+def test_process_mesh_rejects_bad_ids(pkg, gpu):
+    from conftest import rect_tri_mesh
+
+    V, tri, markers = rect_tri_mesh(6, 5, seed=5)
+    tri[3, 1] = len(V) + 1
+    with pytest.raises(pkg.RbffdError):
+        pkg.processmesh_arrays(V, tri, markers)

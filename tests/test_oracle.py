@@ -193,3 +193,38 @@ def test_singular_and_bad_input(pkg, orc):
     assert e.value.code == orc.ORC_ESINGULAR
     with pytest.raises(orc.OracleError):
         orc.generate(X, X, 3, len(X) + 1, 2, ("E",))
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_process_mesh_oracle_against_numpy(orc, reverse):
+    """processmesh after the file reads (src/processmesh.jl:1-192): the oracle's centroids,
+    midpoints, normals and tangents equal a numpy restatement bit for bit; the nearest
+    centroids are checked by brute force; normals end up pointing out of the square whichever
+    way the boundary is listed; ghost nodes sit one offset outside the midpoints."""
+    from conftest import rect_tri_mesh
+
+    V, tri, markers = rect_tri_mesh(12, 9, seed=3, reverse=reverse)
+    bc = np.concatenate(markers)
+    Y, nrm, tng, off = orc.process_mesh(V, tri, bc)
+    ntri, nbc = len(tri), len(bc)
+    a, b, c = V[tri[:, 0] - 1], V[tri[:, 1] - 1], V[tri[:, 2] - 1]
+    C = (a + b + c) / 3.0
+    assert np.array_equal(Y[:ntri], C)
+    p, q = V[bc[:, 0] - 1], V[bc[:, 1] - 1]
+    M = (p + q) / 2.0
+    assert np.array_equal(Y[ntri:ntri + nbc], M)
+    d = q - p
+    ln = np.sqrt(d[:, 1] * d[:, 1] + d[:, 0] * d[:, 0])
+    n0 = np.stack([-d[:, 1] / ln, d[:, 0] / ln], axis=1)
+    t0 = np.stack([d[:, 0] / ln, d[:, 1] / ln], axis=1)
+    d2 = ((M[:, None, :] - C[None, :, :]) ** 2).sum(-1)
+    nn = d2.argmin(1)
+    sg = np.sign(np.dot(M[0] - C[nn[0]], n0[0]))
+    assert np.array_equal(nrm, sg * n0) and np.array_equal(tng, sg * t0)
+    assert off == pytest.approx(np.sqrt(d2[np.arange(nbc), nn]).mean(), rel=1e-14)
+    assert np.allclose(Y[ntri + nbc:], M + nrm * off, rtol=0, atol=1e-15)
+    # outward: bottom (0, -1), right (1, 0), top (0, 1), left (-1, 0)
+    k = np.cumsum([0] + [len(m) for m in markers])
+    for (i, want) in enumerate([(0, -1), (1, 0), (0, 1), (-1, 0)]):
+        assert np.allclose(nrm[k[i]:k[i + 1]].mean(0), want, atol=1e-12)
+    assert (Y[ntri + nbc:, 0] < -0.5 * off + 1e-12).sum() == len(markers[3])  # left ghosts outside
