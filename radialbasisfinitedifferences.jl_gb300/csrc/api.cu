@@ -550,15 +550,19 @@ bool build_op_table(const int *ops, int nops, int p, int k_deriv, OpTable *t, st
     t->p = p;
     int closed = 1;
     for (int q = 0; q < nops; q++) {
-        if (ops[q] == RBFFD_OP_DX || ops[q] == RBFFD_OP_DY)
-            closed |= 2;
-        else if (ops[q] == RBFFD_OP_LAP)
-            closed |= 4;
-        else
-            closed = 0;  // any other operator: the term table
+        switch (ops[q]) {
+        case RBFFD_OP_E: break;
+        case RBFFD_OP_DX:
+        case RBFFD_OP_DY: closed |= 2; break;
+        case RBFFD_OP_DXX:
+        case RBFFD_OP_DYY: closed |= 2 | 8; break;
+        case RBFFD_OP_DXY: closed |= 8; break;
+        case RBFFD_OP_LAP: closed |= 4; break;
+        default: closed = 0;  // any other operator: the term table
+        }
         if (!closed) break;
     }
-    t->r3_grad_lap = (RBFFD_RHS_CLOSED && p == 3) ? closed : 0;
+    t->r3_closed = (RBFFD_RHS_CLOSED && p == 3) ? closed : 0;
     bool hv4 = nops > 0;
     for (int q = 0; q < nops; q++) hv4 = hv4 && (ops[q] == RBFFD_OP_DXK || ops[q] == RBFFD_OP_DYK);
     t->r5_hv4 = RBFFD_RHS_CLOSED && p == 5 && k_deriv == 4 && hv4;

@@ -44,10 +44,11 @@ struct OpDesc {
 struct OpTable {
     int nops;
     int p;
-    // Nonzero when p = 3 and every operator is Dx, Dy or Lap: the register Schur kernel then
+    // Nonzero when p = 3 and every operator is E, Dx, Dy, Dxx, Dyy, Dxy or Lap (the
+    // reference's generate_operator set and the Laplacian): the register Schur kernel then
     // forms their right-hand sides from closed forms instead of the term table.  Bit 0 set,
-    // bit 1: some Dx or Dy, bit 2: some Lap.
-    int r3_grad_lap;
+    // bit 1: 3r needed (Dx, Dy, Dxx, Dyy), bit 2: some Lap, bit 3: 3/r needed (Dxx, Dyy, Dxy).
+    int r3_closed;
     // 1 when p = 5, K = 4 and every operator is Dxk or Dyk (the hyperviscosity pair of the
     // time-stepping example): closed forms likewise.
     int r5_hv4;

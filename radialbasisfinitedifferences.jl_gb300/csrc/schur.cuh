@@ -864,7 +864,7 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
 {
     const int r = ops.nops;
     const bool at0 = is_zero64(yx) && is_zero64(yy);
-    const int closed = ops.r3_grad_lap;
+    const int closed = ops.r3_closed;
     for (int i = lane; i < n; i += 32) {
         // y~ - x~_i; at the centre (the collocated case) the negation is a sign flip on the
         // integer pipe instead of an FP64 subtraction from zero
@@ -876,14 +876,30 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
         const double rr = sqrt_nr(r2, y0);
         const double rinv = need_rinv ? recip_nr(rr, y0) : 0.0;
         if (closed) {
-            // d/dx r^3 = 3 x r, d/dy r^3 = 3 y r, and sx^2 d2/dx2 r^3 + sy^2 d2/dy2 r^3
-            // = (3 (2 sx^2 + sy^2) x^2 + 3 (sx^2 + 2 sy^2) y^2) / r (with r^2 = x^2 + y^2):
-            // 8 FP64 operations per node for Dx, Dy and Lap after r and 1/r instead of 17
+            // r^3 = r^2 r; d/dx r^3 = 3 x r; d2/dx2 r^3 = 3 r + 3 x^2 / r; d2/dxdy r^3 = 3 x y / r
+            // (y alike); sx^2 d2/dx2 r^3 + sy^2 d2/dy2 r^3 = (3 (2 sx^2 + sy^2) x^2
+            // + 3 (sx^2 + 2 sy^2) y^2) / r (with r^2 = x^2 + y^2).  For Dx, Dy and Lap: 8 FP64
+            // operations per node after r and 1/r instead of 17.
             const double t3 = (closed & 2) ? 3.0 * rr : 0.0;
+            const double q3 = (closed & 8) ? 3.0 * rinv : 0.0;
             const double lap = (closed & 4) ? fma(sc[2 * r] * cx, cx, (sc[2 * r + 1] * cy) * cy) * rinv : 0.0;
             for (int q = 0; q < r; q++) {
                 const OpDesc &od = ops.op[q];
-                B[i * r + q] = od.ncomp == 2 ? lap : t3 * (od.c[0].a ? cx : cy);
+                const int oa = od.c[0].a, ob = od.c[0].b;
+                double v;
+                if (od.ncomp == 2)
+                    v = lap;  // Lap
+                else if (oa + ob == 0)
+                    v = r2 * rr;  // E
+                else if (oa + ob == 1)
+                    v = t3 * (oa ? cx : cy);  // Dx, Dy
+                else if (oa == 1)
+                    v = (q3 * cx) * cy;  // Dxy
+                else {
+                    const double c = oa ? cx : cy;  // Dxx, Dyy
+                    v = fma(q3 * c, c, t3);
+                }
+                B[i * r + q] = v;
             }
             continue;
         }
@@ -929,16 +945,18 @@ __device__ __forceinline__ void build_rhs_schur(const OpTable &ops, const double
         return;
     }
     if (closed && at0) {
-        // the polynomial rows at the centre: 1 at x (Dx) or y (Dy); 2 sx^2 at x^2 and 2 sy^2
-        // at y^2 (Lap); zero elsewhere
+        // the polynomial rows at the centre: a! b! at the monomial x^a y^b of the operator
+        // d^(a+b)/dx^a dy^b (index (a + b)(a + b + 1)/2 + b), zero elsewhere; 2 sx^2 at x^2 and
+        // 2 sy^2 at y^2 for Lap
         for (int l = lane; l < m; l += 32)
             for (int q = 0; q < r; q++) {
                 const OpDesc &od = ops.op[q];
+                const int oa = od.c[0].a, ob = od.c[0].b, t = oa + ob;
                 double v = 0.0;
                 if (od.ncomp == 2)
                     v = l == 3 ? twice64(sc[2 * q]) : l == 5 ? twice64(sc[2 * q + 1]) : 0.0;
-                else if (l == (od.c[0].a ? 1 : 2))
-                    v = 1.0;
+                else if (l == t * (t + 1) / 2 + ob)
+                    v = (oa == 2 || ob == 2) ? 2.0 : 1.0;
                 B[(n + l) * r + q] = v;
             }
         __syncwarp();
@@ -1076,7 +1094,7 @@ __global__ void __launch_bounds__(RBFFD_SCHUR_MAX_THREADS(SP), 1) solve_mixed_sc
         if (lane < 2 * r) {
             const int q = lane >> 1, c = lane & 1;
             if (c < ops.op[q].ncomp) sc[lane] = ipow(sx, ops.op[q].c[c].a) * ipow(sy, ops.op[q].c[c].b);
-        } else if ((ops.r3_grad_lap & 4) && lane < 2 * r + 2) {
+        } else if ((ops.r3_closed & 4) && lane < 2 * r + 2) {
             // the closed-form Lap of r^3: 3 (2 sx^2 + sy^2) and 3 (sx^2 + 2 sy^2)
             const double sx2 = sx * sx, sy2 = sy * sy;
             sc[lane] = 3.0 * (lane == 2 * r ? twice64(sx2) + sy2 : sx2 + twice64(sy2));
