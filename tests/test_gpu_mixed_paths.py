@@ -8,8 +8,10 @@
 * The shared-memory mixed kernel, which takes what the register kernels do not: stencils of
   more than 64 nodes, more than 32 monomials, or more than 8 operators.
 * The closed-form right-hand sides of the register kernel (PHS r^3 with every operator in
-  {Dx, Dy, Lap}): operator subsets and orders, stencil sizes of each register instantiation,
-  and evaluation points off the nodes (rows that share a nearest node's factorisation).
+  {E, Dx, Dy, Dxx, Dyy, Dxy, Lap}, and r^5 with the K = 4 pair Dxk/Dyk): operator subsets and
+  orders, stencil sizes of each register instantiation, and evaluation points off the nodes
+  (rows that share a nearest node's factorisation).  The full r^3 set is also covered by
+  test_gpu_parity.py::test_weights_all_ops.
 
 Bars as in test_gpu_parity.py: 1e-9 row-relative for mixed weights of well-conditioned
 systems (PHS r^3, degree <= 3), 5e-9 for r^5 or degree >= 4 (where the oracle's explicit
